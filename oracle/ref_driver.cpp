@@ -1,0 +1,259 @@
+// C-ABI driver around the reference's own CPU implementation of the
+// Barnes-Hut path (projects/nbody_core), compiled from the reference sources
+// in place by oracle/build_ref.sh into oracle/_ref/libngrav_ref.so.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker's window onto the real
+// reference: tests/golden/make_golden.py calls it to produce the golden
+// fixtures that pin the C restatement (oracle/ngrav_oracle.c) and the CUDA
+// path. The product library never links or loads it.
+//
+// Every entry point forwards to the reference's public API unchanged:
+//   ref_plummer         -> ngrav::ic::Plummer<3>            (include/ngrav/ic/Plummer.hpp:26-112)
+//   ref_direct_accel    -> ngrav::ComputeAccelDirect<3>      (src/Solvers.cpp:77-106)
+//   ref_bh_accel        -> AdaptiveTree<3>(v, ncrit) + ComputeQuadrupoles + ComputeAccelBarnesHut<3>
+//                          (src/Tree.cpp:33-52,205-254; src/Solvers.cpp:407-415)
+//   ref_tree_*          -> AdaptiveTree<3> node arrays      (include/ngrav/Tree.hpp:44-63)
+//   ref_leapfrog        -> ngrav::LeapfrogStep<3>           (src/Integrator.cpp:9-39)
+//   ref_diagnostics     -> System<3>::TotalEnergy / CenterOfMass / AngularMomentum
+//                          (include/ngrav/System.hpp:119-193) and the momentum sum of
+//                          DeckSim::Snapshot (src/DeckSim.cpp:147-153)
+#include "ngrav/Integrator.hpp"
+#include "ngrav/Solvers.hpp"
+#include "ngrav/System.hpp"
+#include "ngrav/Tree.hpp"
+#include "ngrav/ic/Plummer.hpp"
+
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+using namespace ngrav;
+
+namespace {
+
+SoA<3> MakeSoA(int n, const double* x, const double* y, const double* z, const double* m) {
+    SoA<3> s;
+    s.Resize(static_cast<std::size_t>(n));
+    for (int i = 0; i < n; ++i) {
+        s.x[i] = x[i];
+        s.y[i] = y[i];
+        s.z[i] = z[i];
+        s.m[i] = m[i];
+    }
+    return s;
+}
+
+StepParams MakeParams(double G, double eps, double theta) {
+    StepParams sp;
+    sp.G = G;
+    sp.soft = Softening::Plummer(eps);
+    sp.mac.theta = theta;
+    sp.mac.kind = MacKind::Geometric;
+    sp.solver = Solver::BarnesHut;
+    return sp;
+}
+
+struct TreeHandle {
+    AdaptiveTree<3>* tree;
+};
+
+} // namespace
+
+extern "C" {
+
+int ref_plummer(int n, unsigned seed, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                double* m) {
+    ic::PlummerParams pp;
+    pp.n = n;
+    pp.seed = seed;
+    const SoA<3> s = ic::Plummer<3>(pp);
+    for (int i = 0; i < n; ++i) {
+        x[i] = s.x[i];
+        y[i] = s.y[i];
+        z[i] = s.z[i];
+        vx[i] = s.vx[i];
+        vy[i] = s.vy[i];
+        vz[i] = s.vz[i];
+        m[i] = s.m[i];
+    }
+    return 0;
+}
+
+void ref_direct_accel(int n, const double* x, const double* y, const double* z, const double* m, double G,
+                      double eps, double* ax, double* ay, double* az) {
+    const SoA<3> s = MakeSoA(n, x, y, z, m);
+    SoA<3> out;
+    ComputeAccelDirect<3>(ViewOf(s), MakeParams(G, eps, 0.5), out);
+    std::memcpy(ax, out.ax.data(), sizeof(double) * n);
+    std::memcpy(ay, out.ay.data(), sizeof(double) * n);
+    std::memcpy(az, out.az.data(), sizeof(double) * n);
+}
+
+// quad != 0: monopole + quadrupole (the deck/System path); quad == 0: monopole only.
+// Returns the wall time of the tree build + quadrupoles + walk in milliseconds.
+double ref_bh_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
+                    double theta, int ncrit, int quad, double* ax, double* ay, double* az) {
+    const SoA<3> s = MakeSoA(n, x, y, z, m);
+    const PosMassView<3> v = ViewOf(s);
+    const StepParams sp = MakeParams(G, eps, theta);
+    SoA<3> out;
+    const auto t0 = std::chrono::steady_clock::now();
+    AdaptiveTree<3> tree(v, ncrit);
+    if (quad) tree.ComputeQuadrupoles(v);
+    ComputeAccelBarnesHut<3>(v, sp, tree, {}, out);
+    const auto t1 = std::chrono::steady_clock::now();
+    std::memcpy(ax, out.ax.data(), sizeof(double) * n);
+    std::memcpy(ay, out.ay.data(), sizeof(double) * n);
+    std::memcpy(az, out.az.data(), sizeof(double) * n);
+    return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+void* ref_tree_build(int n, const double* x, const double* y, const double* z, const double* m, int ncrit,
+                     int maxDepth, int* numNodes) {
+    const SoA<3> s = MakeSoA(n, x, y, z, m);
+    const PosMassView<3> v = ViewOf(s);
+    auto* h = new TreeHandle{new AdaptiveTree<3>(v, ncrit, maxDepth)};
+    h->tree->ComputeQuadrupoles(v);
+    *numNodes = h->tree->NumNodes();
+    return h;
+}
+
+// Node arrays in the reference's own (creation-order) numbering plus the
+// derived (level, octant-path prefix, subtree count) needed for a canonical,
+// numbering-independent comparison. prefix holds 3 bits per level, root = 0.
+void ref_tree_export(void* handle, int n, int* level, unsigned long long* prefix, int* count, int* isLeaf,
+                     double* center, double* half, double* com, double* mass, double* maxRadius, double* quad,
+                     int* order, int* parent, int* firstParticle) {
+    const AdaptiveTree<3>& t = *static_cast<TreeHandle*>(handle)->tree;
+    const int nn = t.NumNodes();
+    std::vector<int> cnt(static_cast<std::size_t>(nn), 0);
+    for (int i = 0; i < nn; ++i) {
+        if (t.IsLeaf(i)) cnt[i] = t.particleCount[i];
+    }
+    for (int i = nn - 1; i > 0; --i) cnt[t.parent[i]] += cnt[i];
+    for (int i = 0; i < nn; ++i) {
+        if (i == 0) {
+            level[i] = 0;
+            prefix[i] = 0ull;
+        } else {
+            const int p = t.parent[i];
+            int oct = -1;
+            for (int c = 0; c < 8; ++c)
+                if (t.children[p][c] == i) oct = c;
+            level[i] = level[p] + 1;
+            prefix[i] = (prefix[p] << 3) | static_cast<unsigned long long>(oct);
+        }
+        count[i] = cnt[i];
+        isLeaf[i] = t.IsLeaf(i) ? 1 : 0;
+        center[3 * i + 0] = t.center[i].x;
+        center[3 * i + 1] = t.center[i].y;
+        center[3 * i + 2] = t.center[i].z;
+        half[i] = t.halfSize[i];
+        com[3 * i + 0] = t.com[i].x;
+        com[3 * i + 1] = t.com[i].y;
+        com[3 * i + 2] = t.com[i].z;
+        mass[i] = t.mass[i];
+        maxRadius[i] = t.maxRadius[i];
+        quad[5 * i + 0] = t.Qxx[i];
+        quad[5 * i + 1] = t.Qyy[i];
+        quad[5 * i + 2] = t.Qxy[i];
+        quad[5 * i + 3] = t.Qxz[i];
+        quad[5 * i + 4] = t.Qyz[i];
+        parent[i] = t.parent[i];
+        firstParticle[i] = t.firstParticle[i];
+    }
+    for (int k = 0; k < n; ++k) order[k] = t.order[k];
+}
+
+void ref_tree_free(void* handle) {
+    auto* h = static_cast<TreeHandle*>(handle);
+    delete h->tree;
+    delete h;
+}
+
+// KDK leapfrog through the reference's LeapfrogStep with a Barnes-Hut
+// AccelFn at leaf capacity `ncrit` (the System path hard-wires ncrit 8,
+// include/ngrav/System.hpp:57). If primed == 0 the acceleration is computed
+// first, as System::Prime does. State arrays are updated in place. Returns
+// the wall time of the nsteps steps in milliseconds.
+double ref_leapfrog(int n, double* x, double* y, double* z, double* vx, double* vy, double* vz, const double* m,
+                    double* ax, double* ay, double* az, double G, double eps, double theta, int ncrit, double dt,
+                    int nsteps, int primed) {
+    SoA<3> s = MakeSoA(n, x, y, z, m);
+    for (int i = 0; i < n; ++i) {
+        s.vx[i] = vx[i];
+        s.vy[i] = vy[i];
+        s.vz[i] = vz[i];
+        s.ax[i] = ax[i];
+        s.ay[i] = ay[i];
+        s.az[i] = az[i];
+    }
+    StepParams sp = MakeParams(G, eps, theta);
+    sp.dt = dt;
+    const AccelFn<3> accel = [ncrit](const SoA<3>& in, const StepParams& p, SoA<3>& o) {
+        const PosMassView<3> v = ViewOf(in);
+        AdaptiveTree<3> tree(v, ncrit);
+        tree.ComputeQuadrupoles(v);
+        ComputeAccelBarnesHut<3>(v, p, tree, {}, o);
+    };
+    if (!primed) {
+        SoA<3> tmp;
+        accel(s, sp, tmp);
+        s.ax = tmp.ax;
+        s.ay = tmp.ay;
+        s.az = tmp.az;
+    }
+    SoA<3> scratch;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int k = 0; k < nsteps; ++k) LeapfrogStep<3>(s, sp, accel, scratch);
+    const auto t1 = std::chrono::steady_clock::now();
+    for (int i = 0; i < n; ++i) {
+        x[i] = s.x[i];
+        y[i] = s.y[i];
+        z[i] = s.z[i];
+        vx[i] = s.vx[i];
+        vy[i] = s.vy[i];
+        vz[i] = s.vz[i];
+        ax[i] = s.ax[i];
+        ay[i] = s.ay[i];
+        az[i] = s.az[i];
+    }
+    return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+// out[0] = total energy (O(N^2) potential), out[1..3] = centre of mass,
+// out[4..6] = angular momentum about the COM, out[7..9] = linear momentum.
+void ref_diagnostics(int n, const double* x, const double* y, const double* z, const double* vx, const double* vy,
+                     const double* vz, const double* m, double G, double eps, double* out) {
+    SoA<3> s = MakeSoA(n, x, y, z, m);
+    for (int i = 0; i < n; ++i) {
+        s.vx[i] = vx[i];
+        s.vy[i] = vy[i];
+        s.vz[i] = vz[i];
+    }
+    System<3> sys;
+    sys.SetParticles(std::move(s));
+    const StepParams sp = MakeParams(G, eps, 0.5);
+    out[0] = sys.TotalEnergy(sp);
+    const glm::dvec3 c = sys.CenterOfMass();
+    out[1] = c.x;
+    out[2] = c.y;
+    out[3] = c.z;
+    const glm::dvec3 L = sys.AngularMomentum();
+    out[4] = L.x;
+    out[5] = L.y;
+    out[6] = L.z;
+    const SoA<3>& st = sys.State();
+    double px = 0.0, py = 0.0, pz = 0.0;
+    for (int i = 0; i < n; ++i) {
+        px += st.m[i] * st.vx[i];
+        py += st.m[i] * st.vy[i];
+        pz += st.m[i] * st.vz[i];
+    }
+    out[7] = px;
+    out[8] = py;
+    out[9] = pz;
+}
+
+} // extern "C"
