@@ -1,0 +1,292 @@
+#!/usr/bin/env python
+"""Headline benchmark: Barnes-Hut KDK particle-steps/s on one GB300.
+
+Workload (default): the two-component galaxy, N = 4,194,304 (Hernquist halo
+3,774,874 + exponential disk 419,430), G = 1, eps = 0.002, dt = 2e-4,
+monopole+quadrupole, split precision, plain theta-MAC.  A step is one KDK
+leapfrog step (kick-drift, 63-bit keys, radix sort, octree, moments, grouped
+walk with P2P/P2C, closing kick) over the whole system.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   = N * K / (device time of the K timed steps, CUDA events on the
+          engine's stream), inputs resident in HBM.
+e2e     = the same metric through the reference-facing C-ABI with host
+          buffers: per step ngrav_gpu_set_particles_f32 from pinned host
+          memory + ngrav_gpu_compute_accel into pinned FP64 host arrays
+          (the ComputeAccelBarnesHut contract), wall clock.
+roofline: the walk kernel (P2P + P2C, FP32 pipe): algorithmic flops
+          (20 per P2P pair + 60 per P2C term, device-counted) / its
+          event-timed duration, against the measured FP32 FMA peak.
+cpu_baseline: the oracle (C restatement of the reference's CPU path) on the
+          host cores, bounded sample: full tree build + walk over every
+          k-th leaf group, extrapolated to a full step.
+With --gpus N > 1 (torchrun), each rank runs an independent replica (the
+path has no data-parallel split on one system); value sums the replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as ge  # noqa: E402
+
+WORKLOADS = {
+    # name: (generator, kwargs, eps, dt, theta, leaf capacity)
+    "galaxy4m": ("galaxy", {}, 0.002, 2e-4, 0.6, 16),
+    "plummer1m": ("plummer", {"n": 1048576, "seed": 1}, 0.005, 5e-4, 0.5, 16),
+    "plummer16k": ("plummer", {"n": 16384, "seed": 0}, 0.01, 1e-3, 0.5, 16),
+}
+METRIC = "particle-steps/s at N=4M, learned-MAC vs plain θ-MAC at equal 1e-3 rms force err"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+        self._t = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self._proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        if self._t:
+            self._t.join(timeout=5)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_inputs(pkg_ic, workload):
+    gen, kw, eps, dt, theta, ncrit = WORKLOADS[workload]
+    arrs = getattr(pkg_ic, gen)(**kw)
+    return arrs, eps, dt, theta, ncrit
+
+
+def cpu_baseline(orc, arrs, eps, theta, ncrit, target_s=15.0):
+    """Oracle on the host cores: full tree + a strided sample of leaf groups."""
+    O = orc.Oracle()
+    x, y, z, _, _, _, m = (a.astype(np.float64) for a in arrs)
+    n = len(x)
+    stride = max(1, int(n // 65536))
+    build_ms, walk_ms, frac, _ = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride)
+    # grow the sample while it is short of the target
+    while build_ms + walk_ms < 1e3 * target_s * 0.3 and stride > 1:
+        stride = max(1, stride // 4)
+        build_ms, walk_ms, frac, _ = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride)
+    step_ms = build_ms + walk_ms / max(frac, 1e-12)
+    return {"value": n / (step_ms * 1e-3), "unit": "particle-steps/s", "cores": O.num_threads(),
+            "kind": "port", "step_ms_extrapolated": step_ms,
+            "sample": f"N={n}: full FP64 tree build ({build_ms:.0f} ms) + grouped walk over every "
+                      f"{stride}-th leaf group ({100 * frac:.1f}% of particles, {walk_ms:.0f} ms), "
+                      f"extrapolated to one full force evaluation"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    orc = ge.load_oracle()
+    orc.build_oracle()
+    ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
+    arrs, eps, dt, theta, ncrit = make_inputs(ic, args.workload)
+    O = orc.Oracle()
+    x, y, z, _, _, _, m = (a.astype(np.float64) for a in arrs)
+    n = len(x)
+    stride = max(1, int(n // 16384))
+    times = []
+    for k in range(args.warmup + args.steps):
+        build_ms, walk_ms, frac, _ = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride)
+        if k >= args.warmup:
+            times.append(build_ms + walk_ms / max(frac, 1e-12))
+    step_ms = float(np.mean(times))
+    value = n / (step_ms * 1e-3)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "replicas", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "n": n, "theta": theta, "eps": eps, "leaf_capacity": ncrit},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": f"each step: full FP64 tree build + grouped walk over every {stride}-th "
+                                       f"leaf group, extrapolated to one full KDK force evaluation"},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="galaxy4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--theta", type=float, default=None)
+    ap.add_argument("--precision", default="split", choices=["split", "plain"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    pkg = ge.load_package()
+    ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"])
+    dev = local
+    arrs, eps, dt, theta, ncrit = make_inputs(ic, args.workload)
+    if args.theta is not None:
+        theta = args.theta
+    n = len(arrs[0])
+    prec = pkg.PRECISION_SPLIT if args.precision == "split" else pkg.PRECISION_PLAIN
+    sim = pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=ncrit, precision=prec,
+                          device=dev, timing=True)
+    sim.set_particles_f32(*arrs)
+    sim.prime()
+    sim.step(args.warmup, dt)
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(dev)
+        tdist.init_process_group("nccl")
+        dist = tdist
+        dist.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    sim.reset_cumulative()
+    sim.step(args.steps, dt)
+    st = sim.stats()
+    clk = clocks.stop()
+    ms_step = st["cum_ms_step"] / args.steps
+    ms_max = ms_step
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms_step], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * n / (ms_max * 1e-3)
+
+    # roofline of the walk kernel
+    flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
+    walk_s = st["cum_ms_walk"] * 1e-3
+    achieved = flops / walk_s / 1e12 if walk_s > 0 else None
+    peak = pkg.probe_fp32_peak(dev)
+    force = sim.force_error(nsample=4096, seed=2024, fp64_pairs=False)
+
+    # e2e: host buffers through the C-ABI, wall clock
+    e2e = None
+    h2d = 7 * 4 * n
+    d2h = 3 * 8 * n
+    try:
+        import torch
+        pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() for a in arrs]
+        outs = [torch.empty(n, dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+    except Exception:
+        pinned = [np.ascontiguousarray(a) for a in arrs]
+        outs = [np.empty(n) for _ in range(3)]
+    x0 = sim.state()  # keep the stepped state for reporting
+    del x0
+    import ctypes
+    fptr = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) for a in pinned]
+    dptr = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in outs]
+    L = sim.L
+    t_e2e = []
+    for k in range(1 + args.e2e_steps):
+        t0 = time.perf_counter()
+        rc = L.ngrav_gpu_set_particles_f32(sim.h, n, *fptr)
+        rc |= L.ngrav_gpu_compute_accel(sim.h, *dptr)
+        t1 = time.perf_counter()
+        if rc:
+            raise RuntimeError("e2e call failed: " + L.ngrav_gpu_last_error(sim.h).decode())
+        if k > 0:
+            t_e2e.append(t1 - t0)
+    e2e_ms = 1e3 * float(np.mean(t_e2e))
+    e2e = {"value": world * n / (e2e_ms * 1e-3), "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+           "call": "ngrav_gpu_set_particles_f32 + ngrav_gpu_compute_accel (pinned host buffers)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(ge.load_oracle(), arrs, eps, theta, ncrit)
+        except Exception as exc:  # the baseline must not sink the GPU line
+            cpu = {"error": str(exc)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded galaxy generator)" if args.workload == "galaxy4m" else "synthetic",
+            "config": {"workload": args.workload, "n": n, "mac": "geometric", "theta": theta, "eps": eps, "dt": dt,
+                       "leaf_capacity": ncrit, "precision": args.precision, "quadrupole": True,
+                       "parallelism": "replicas" if world > 1 else "single-gpu",
+                       "l2": "per-step working set > 0.5 GB, larger than the 129 MB L2",
+                       "force_err_rms": force["rms"], "force_err_max": force["max"],
+                       "force_err_median": force["median"], "force_err_targets": force["nsample"],
+                       "interactions_per_s": (st["cum_p2p_pairs"] + st["cum_p2c_terms"]) / (st["cum_ms_step"] * 1e-3),
+                       "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
+                       "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
+                       "ms_walk_per_step": st["cum_ms_walk"] / max(1, st["cum_evals"]),
+                       "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"])},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                         "kernel": "walk_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
+                         "peak_source": "measured FP32 FMA probe (ngrav_gpu_probe_fp32_peak)"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,202 @@
+/*
+ * ngrav_gpu.h -- C-ABI of the GB300 Barnes-Hut force evaluation and KDK step.
+ *
+ * A drop-in replacement for the force/step path of HasanHelal429/OpenGL-Physics
+ * projects/nbody_core.  Every entry point is extern "C", takes plain pointers
+ * and sizes, never throws, and returns an int status (NGRAV_OK == 0);
+ * ngrav_gpu_last_error() gives the text of the last failure on a context.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   System<3>::SetParticles          include/ngrav/System.hpp:29-35   -> ngrav_gpu_set_particles
+ *   System<3>::ComputeAccel (BH)     include/ngrav/System.hpp:43-66   -> ngrav_gpu_compute_accel
+ *   ComputeAccelBarnesHut(v, sp, out) include/ngrav/Solvers.hpp:56-57 -> ngrav_gpu_compute_accel
+ *   AccelFn<3> adapter               include/ngrav/Integrator.hpp:13-14 -> ngrav_gpu_compute_accel
+ *   System<3>::Prime                 include/ngrav/System.hpp:82-85   -> ngrav_gpu_prime
+ *   System<3>::Step / LeapfrogStep   include/ngrav/System.hpp:89-108, src/Integrator.cpp:9-39
+ *                                                                      -> ngrav_gpu_step
+ *   System<3>::State                 include/ngrav/System.hpp:194     -> ngrav_gpu_get_state
+ *   System<3>::TotalEnergy / CenterOfMass / AngularMomentum, the momentum
+ *     sum of DeckSim::Snapshot       include/ngrav/System.hpp:119-193, src/DeckSim.cpp:132-153
+ *                                                                      -> ngrav_gpu_diagnostics
+ *   GpuBarnesHutStats                include/ngrav/gpu/GpuBarnesHut.hpp:23-31 -> ngrav_gpu_get_stats
+ *   AdaptiveTree<3> node arrays      include/ngrav/Tree.hpp:44-63      -> ngrav_gpu_debug_tree
+ *   the force-error measure of --bench  projects/02_nbody_gravity/src/main.cpp:313-331
+ *                                                                      -> ngrav_gpu_force_error
+ *
+ * Threading: one context per host thread.  Calls are synchronous: every
+ * entry point has finished its GPU work when it returns.
+ */
+#ifndef NGRAV_GPU_H
+#define NGRAV_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NGRAV_GPU_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    NGRAV_OK = 0,
+    NGRAV_ERR_INVALID_ARG = 1,   /* bad pointer, size or option */
+    NGRAV_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    NGRAV_ERR_NO_PARTICLES = 3,  /* no particle set on the context */
+    NGRAV_ERR_CAPACITY = 4,      /* node pool or walk stack overflow that could not be grown */
+    NGRAV_ERR_NONFINITE = 5,     /* NaN/Inf in positions or masses */
+    NGRAV_ERR_OOM = 6,           /* device allocation failed */
+    NGRAV_ERR_TIMEOUT = 7,       /* a bounded device wait ran out */
+    NGRAV_ERR_DEPTH = 8          /* strict_depth set and a leaf needs more than 21 levels */
+};
+
+/* Multipole acceptance criterion (include/ngrav/Mac.hpp:8-11). */
+enum { NGRAV_MAC_GEOMETRIC = 0, NGRAV_MAC_LEARNED = 1 };
+
+/* Precision of the particle state and of the force sums.
+ * PLAIN: FP32 absolute positions, plain FP32 accumulation.
+ * SPLIT: positions kept as double-float (hi + lo) pairs, force evaluation on
+ *        FP32 offsets from each leaf cell's centre, Kahan-compensated
+ *        per-target accumulators. */
+enum { NGRAV_PRECISION_PLAIN = 0, NGRAV_PRECISION_SPLIT = 1 };
+
+typedef struct ngrav_gpu_opts {
+    int abi_version;       /* NGRAV_GPU_ABI_VERSION */
+    int device;            /* CUDA device ordinal */
+    int leaf_capacity;     /* ncrit: a leaf splits when it would hold more (Tree.hpp:38; default 8) */
+    int max_depth;         /* maxDepth of AdaptiveTree (default 40); keys resolve 21 levels */
+    int quadrupole;        /* 1: monopole + quadrupole far field (the System path), 0: monopole */
+    int mac;               /* NGRAV_MAC_* */
+    int precision;         /* NGRAV_PRECISION_* */
+    int fp64_mac_retest;   /* 1: re-decide borderline FP32 opening tests in FP64 */
+    int strict_depth;      /* 1: a leaf deeper than 21 levels is an error, 0: counted in stats */
+    int timing;            /* 1: record per-phase CUDA-event times in ngrav_gpu_stats */
+    double G;              /* gravitational constant (StepParams::G) */
+    double eps;            /* Plummer softening length (Softening::eps) */
+    double theta;          /* opening angle (MacParams::theta) */
+} ngrav_gpu_opts;
+
+typedef struct ngrav_gpu_diag {
+    double kinetic;        /* sum 1/2 m v^2 */
+    double potential;      /* pair potential sum (exact O(N^2) FP64, or tree estimate) */
+    double energy;         /* kinetic + potential (System::TotalEnergy) */
+    double com[3];         /* centre of mass */
+    double L[3];           /* angular momentum about the COM */
+    double P[3];           /* linear momentum */
+    int potential_exact;   /* 1 if the potential is the exact pairwise sum */
+} ngrav_gpu_diag;
+
+typedef struct ngrav_gpu_ferr {
+    double rms;            /* rms of |a - a_ref| / |a_ref| over the sampled targets */
+    double max;
+    double median;
+    int nsample;
+} ngrav_gpu_ferr;
+
+typedef struct ngrav_gpu_stats {
+    /* last force evaluation (milliseconds; 0 unless opts.timing) */
+    double ms_bbox_keys, ms_sort, ms_build, ms_moments, ms_walk, ms_kick, ms_total;
+    /* interaction counts of the last force evaluation (device counters) */
+    long long p2p_pairs;   /* softened particle-particle terms (self excluded) */
+    long long p2c_terms;   /* far-node terms */
+    long long mac_tests;   /* opening tests on internal nodes */
+    long long mac_retests; /* borderline tests re-decided in FP64 */
+    long long groups;      /* target groups (leaves) walked */
+    int nodes, leaves, levels, max_leaf_count;
+    int depth_limited_leaves; /* leaves at the 21-level key limit holding > leaf_capacity */
+    int walk_stack_max;
+    unsigned status_bits;  /* raw device status word of the last evaluation */
+    long long force_evals; /* force evaluations since the context was created */
+    long long n;
+    /* cumulative since ngrav_gpu_reset_cumulative (CUDA-event times on the
+     * context's stream; the per-phase ones need opts.timing) */
+    long long cum_evals;
+    long long cum_p2p_pairs, cum_p2c_terms;
+    double cum_ms_walk;    /* walk kernel (P2P + P2C + closing kick) */
+    double cum_ms_eval;    /* whole force evaluations */
+    double cum_ms_step;    /* ngrav_gpu_step calls, first to last kernel */
+    long long cum_launches; /* kernels this context launched */
+} ngrav_gpu_stats;
+
+typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;
+
+/* Fill opts with the reference defaults: leaf_capacity 8, max_depth 40,
+ * quadrupole on, geometric MAC, theta 0.5, G 1, eps 0.05 (StepParams,
+ * include/ngrav/Solvers.hpp:22-27), split precision, FP64 retest on. */
+int ngrav_gpu_default_opts(ngrav_gpu_opts* opts);
+
+int ngrav_gpu_create(ngrav_gpu_ctx** ctx, const ngrav_gpu_opts* opts);
+void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx);
+const char* ngrav_gpu_last_error(const ngrav_gpu_ctx* ctx);
+
+/* Change G, eps, theta, leaf capacity, MAC or precision between calls. */
+int ngrav_gpu_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* opts);
+
+/* Copy a particle set in (the caller keeps its arrays).  FP64 in, so the
+ * SoA<3> layout maps 1:1; positions are held as double-float pairs in SPLIT
+ * precision and rounded to FP32 in PLAIN.  Velocities and masses are FP32 on
+ * the device.  vx/vy/vz may be NULL (zero velocity).  Resets acceleration
+ * and the primed flag, as System::SetParticles does. */
+int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* z,
+                            const double* vx, const double* vy, const double* vz, const double* m);
+/* FP32 variant: no conversion, for large N. */
+int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
+                                const float* vx, const float* vy, const float* vz, const float* m);
+
+/* One force evaluation on the current positions, written in the caller's
+ * original particle order, G included -- the contract of
+ * ComputeAccelBarnesHut(pts, sp, out).  Does not advance or prime the state. */
+int ngrav_gpu_compute_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az);
+
+/* a(t) for the first half-kick (System::Prime). */
+int ngrav_gpu_prime(ngrav_gpu_ctx* ctx);
+
+/* nsteps kick-drift-kick steps of length dt, device resident (primes first
+ * if needed).  Equivalent to nsteps calls of System::Step with the fixed
+ * global scheme. */
+int ngrav_gpu_step(ngrav_gpu_ctx* ctx, int nsteps, double dt);
+
+/* Read the state back in original particle order.  Any pointer may be NULL. */
+int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, double* vx, double* vy, double* vz);
+int ngrav_gpu_get_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az);
+
+/* FP64 conservation diagnostics of the current state.  exact_potential:
+ * 1 = exact O(N^2) pairwise potential on the GPU, 0 = let the library choose
+ * (exact up to 262,144 particles). */
+int ngrav_gpu_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_diag* out);
+
+/* rms / max / median relative error of the current accelerations against a
+ * direct sum with FP64 accumulation over nsample uniformly drawn targets
+ * (seeded; nsample <= n).  fp64_pairs = 1 evaluates every pair term in FP64,
+ * 0 evaluates pair terms in FP32 and accumulates in FP64. */
+int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp64_pairs, ngrav_gpu_ferr* out);
+
+int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out);
+/* Zero the cum_* fields of ngrav_gpu_stats.  (No reference counterpart:
+ * measurement support.) */
+int ngrav_gpu_reset_cumulative(ngrav_gpu_ctx* ctx);
+
+/* Measured FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA),
+ * from a register-resident FMA-chain kernel timed with CUDA events.  The
+ * denominator of the P2P roofline.  (No reference counterpart: measurement
+ * support.) */
+int ngrav_gpu_probe_fp32_peak(int device, double* tflops);
+
+/* Export the last tree for bit-exact checks.  Call with node arrays NULL to
+ * get *nnodes; then call again with arrays of that size.
+ *   keys[n]        63-bit octant-path key of each particle (original order)
+ *   order[n]       leaf-ordered original indices, ascending within a leaf
+ *                  (AdaptiveTree::order)
+ *   level, prefix  depth and octant path (3 bits per level) of each node
+ *   count          particles under each node; is_leaf
+ *   center[3*nn], half, com[3*nn], mass, max_radius, quad[5*nn] (Qxx Qyy Qxy Qxz Qyz)
+ * Node numbering is the GPU's own; compare in (level, prefix) order. */
+int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* order, int* level, uint64_t* prefix,
+                         int* count, int* is_leaf, double* center, double* half, double* com, double* mass,
+                         double* max_radius, double* quad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NGRAV_GPU_H */

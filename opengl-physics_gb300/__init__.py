@@ -1,0 +1,290 @@
+"""GB300 Barnes-Hut force evaluation and KDK step (Python host side).
+
+A thin ctypes mirror of ``include/ngrav_gpu.h`` that reads like the
+reference's ``ngrav::System<3>`` (projects/nbody_core/include/ngrav/System.hpp):
+
+    sim = NBodySystem(StepParams(G=1.0, eps=0.01, theta=0.5), leaf_capacity=16)
+    sim.set_particles(x, y, z, vx, vy, vz, m)     # System::SetParticles
+    sim.prime()                                     # System::Prime
+    sim.step(nsteps, dt)                            # System::Step (KDK)
+    ax, ay, az = sim.compute_accel()                # ComputeAccelBarnesHut
+    d = sim.diagnostics()                           # TotalEnergy / COM / L / P
+
+All compute runs in ``libngrav_gpu.so`` (hand-written sm_103a kernels).  There
+is no CPU fallback: constructing a system without the library or without a
+GPU raises.  The directory name contains a hyphen, so import it through
+``load()`` or ``importlib`` (module name ``opengl_physics_gb300``).
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libngrav_gpu.so")
+HEADER = os.path.join(os.path.dirname(PKG_DIR), "include", "ngrav_gpu.h")
+
+ABI_VERSION = 1
+OK = 0
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "no particles", 4: "capacity", 5: "non-finite input",
+          6: "out of memory", 7: "timeout", 8: "depth limit"}
+MAC_GEOMETRIC, MAC_LEARNED = 0, 1
+PRECISION_PLAIN, PRECISION_SPLIT = 0, 1
+
+# Every extern "C" entry point declared in include/ngrav_gpu.h.
+EXPORTS = (
+    "ngrav_gpu_default_opts", "ngrav_gpu_create", "ngrav_gpu_destroy", "ngrav_gpu_last_error",
+    "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
+    "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
+    "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
+    "ngrav_gpu_probe_fp32_peak",
+)
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_int), ("device", ctypes.c_int), ("leaf_capacity", ctypes.c_int),
+                ("max_depth", ctypes.c_int), ("quadrupole", ctypes.c_int), ("mac", ctypes.c_int),
+                ("precision", ctypes.c_int), ("fp64_mac_retest", ctypes.c_int), ("strict_depth", ctypes.c_int),
+                ("timing", ctypes.c_int), ("G", ctypes.c_double), ("eps", ctypes.c_double),
+                ("theta", ctypes.c_double)]
+
+
+class Diag(ctypes.Structure):
+    _fields_ = [("kinetic", ctypes.c_double), ("potential", ctypes.c_double), ("energy", ctypes.c_double),
+                ("com", ctypes.c_double * 3), ("L", ctypes.c_double * 3), ("P", ctypes.c_double * 3),
+                ("potential_exact", ctypes.c_int)]
+
+
+class Ferr(ctypes.Structure):
+    _fields_ = [("rms", ctypes.c_double), ("max", ctypes.c_double), ("median", ctypes.c_double),
+                ("nsample", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ms_bbox_keys", ctypes.c_double), ("ms_sort", ctypes.c_double), ("ms_build", ctypes.c_double),
+                ("ms_moments", ctypes.c_double), ("ms_walk", ctypes.c_double), ("ms_kick", ctypes.c_double),
+                ("ms_total", ctypes.c_double), ("p2p_pairs", ctypes.c_longlong), ("p2c_terms", ctypes.c_longlong),
+                ("mac_tests", ctypes.c_longlong), ("mac_retests", ctypes.c_longlong), ("groups", ctypes.c_longlong),
+                ("nodes", ctypes.c_int), ("leaves", ctypes.c_int), ("levels", ctypes.c_int),
+                ("max_leaf_count", ctypes.c_int), ("depth_limited_leaves", ctypes.c_int),
+                ("walk_stack_max", ctypes.c_int), ("status_bits", ctypes.c_uint), ("force_evals", ctypes.c_longlong),
+                ("n", ctypes.c_longlong), ("cum_evals", ctypes.c_longlong), ("cum_p2p_pairs", ctypes.c_longlong),
+                ("cum_p2c_terms", ctypes.c_longlong), ("cum_ms_walk", ctypes.c_double),
+                ("cum_ms_eval", ctypes.c_double), ("cum_ms_step", ctypes.c_double),
+                ("cum_launches", ctypes.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_F = ctypes.POINTER(ctypes.c_float)
+_I = ctypes.POINTER(ctypes.c_int)
+_U64 = ctypes.POINTER(ctypes.c_uint64)
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load_library(path: str | None = None):
+    """Load libngrav_gpu.so (building it if absent) and declare the C-ABI."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.isfile(path):
+        from importlib import util as _u
+        spec = _u.spec_from_file_location("_ngrav_build", os.path.join(PKG_DIR, "build.py"))
+        mod = _u.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = ctypes.CDLL(path)
+    L.ngrav_gpu_default_opts.argtypes = [ctypes.POINTER(Opts)]
+    L.ngrav_gpu_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Opts)]
+    L.ngrav_gpu_destroy.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_destroy.restype = None
+    L.ngrav_gpu_last_error.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_last_error.restype = ctypes.c_char_p
+    L.ngrav_gpu_set_opts.argtypes = [ctypes.c_void_p, ctypes.POINTER(Opts)]
+    L.ngrav_gpu_set_particles.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [_D] * 7
+    L.ngrav_gpu_set_particles_f32.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [_F] * 7
+    L.ngrav_gpu_compute_accel.argtypes = [ctypes.c_void_p, _D, _D, _D]
+    L.ngrav_gpu_prime.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+    L.ngrav_gpu_get_state.argtypes = [ctypes.c_void_p] + [_D] * 6
+    L.ngrav_gpu_get_accel.argtypes = [ctypes.c_void_p] + [_D] * 3
+    L.ngrav_gpu_diagnostics.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Diag)]
+    L.ngrav_gpu_force_error.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.POINTER(Ferr)]
+    L.ngrav_gpu_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+    L.ngrav_gpu_debug_tree.argtypes = [ctypes.c_void_p, _I, _U64, _I, _I, _U64, _I, _I, _D, _D, _D, _D, _D, _D]
+    L.ngrav_gpu_reset_cumulative.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_probe_fp32_peak.argtypes = [ctypes.c_int, _D]
+    _lib = L
+    return L
+
+
+def probe_fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FMA throughput (TFLOP/s) of the device."""
+    L = load_library()
+    out = ctypes.c_double()
+    rc = L.ngrav_gpu_probe_fp32_peak(device, ctypes.byref(out))
+    if rc != OK:
+        raise NgravError(rc, "FP32 peak probe failed")
+    return out.value
+
+
+class NgravError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ngrav_gpu error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+@dataclasses.dataclass
+class StepParams:
+    """Mirror of ngrav::StepParams (include/ngrav/Solvers.hpp:22-36) for the BH path."""
+    G: float = 1.0
+    eps: float = 0.05          # Plummer softening length
+    theta: float = 0.5
+    dt: float = 1e-3
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def _c64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class NBodySystem:
+    """One GPU context; mirrors System<3> for the Barnes-Hut solver."""
+
+    def __init__(self, sp: StepParams | None = None, leaf_capacity: int = 8, precision: int = PRECISION_SPLIT,
+                 quadrupole: bool = True, mac: int = MAC_GEOMETRIC, fp64_mac_retest: bool = True, device: int = 0,
+                 max_depth: int = 40, timing: bool = False, strict_depth: bool = False):
+        self.L = load_library()
+        self.sp = sp or StepParams()
+        o = Opts()
+        self._check(self.L.ngrav_gpu_default_opts(ctypes.byref(o)), None)
+        o.device = device
+        o.leaf_capacity = leaf_capacity
+        o.max_depth = max_depth
+        o.quadrupole = int(quadrupole)
+        o.mac = mac
+        o.precision = precision
+        o.fp64_mac_retest = int(fp64_mac_retest)
+        o.strict_depth = int(strict_depth)
+        o.timing = int(timing)
+        o.G, o.eps, o.theta = self.sp.G, self.sp.eps, self.sp.theta
+        self.opts = o
+        h = ctypes.c_void_p()
+        rc = self.L.ngrav_gpu_create(ctypes.byref(h), ctypes.byref(o))
+        if rc != OK:
+            raise NgravError(rc, "context creation failed (is a CUDA device visible?)")
+        self.h = h
+        self.n = 0
+
+    def _check(self, rc, h):
+        if rc != OK:
+            msg = self.L.ngrav_gpu_last_error(h).decode() if h else ""
+            raise NgravError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ngrav_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_opts(self, **kw):
+        for k, v in kw.items():
+            setattr(self.opts, k, v)
+        self._check(self.L.ngrav_gpu_set_opts(self.h, ctypes.byref(self.opts)), self.h)
+
+    def set_particles(self, x, y, z, vx=None, vy=None, vz=None, m=None):
+        arrs = [_c64(a) for a in (x, y, z, vx, vy, vz, m)]
+        self.n = len(arrs[0])
+        self._check(self.L.ngrav_gpu_set_particles(self.h, self.n, *[_p(a, _D) for a in arrs]), self.h)
+
+    def set_particles_f32(self, x, y, z, vx, vy, vz, m):
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, vx, vy, vz, m)]
+        self.n = len(arrs[0])
+        self._check(self.L.ngrav_gpu_set_particles_f32(self.h, self.n, *[_p(a, _F) for a in arrs]), self.h)
+
+    def compute_accel(self):
+        ax, ay, az = (np.empty(self.n) for _ in range(3))
+        self._check(self.L.ngrav_gpu_compute_accel(self.h, _p(ax, _D), _p(ay, _D), _p(az, _D)), self.h)
+        return ax, ay, az
+
+    def prime(self):
+        self._check(self.L.ngrav_gpu_prime(self.h), self.h)
+
+    def step(self, nsteps=1, dt=None):
+        self._check(self.L.ngrav_gpu_step(self.h, int(nsteps), float(self.sp.dt if dt is None else dt)), self.h)
+
+    def state(self):
+        out = [np.empty(self.n) for _ in range(6)]
+        self._check(self.L.ngrav_gpu_get_state(self.h, *[_p(a, _D) for a in out]), self.h)
+        return tuple(out)
+
+    def accel(self):
+        out = [np.empty(self.n) for _ in range(3)]
+        self._check(self.L.ngrav_gpu_get_accel(self.h, *[_p(a, _D) for a in out]), self.h)
+        return tuple(out)
+
+    def diagnostics(self, exact_potential=False):
+        d = Diag()
+        self._check(self.L.ngrav_gpu_diagnostics(self.h, int(exact_potential), ctypes.byref(d)), self.h)
+        return dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
+                    P=list(d.P), potential_exact=bool(d.potential_exact))
+
+    def force_error(self, nsample=4096, seed=12345, fp64_pairs=False):
+        f = Ferr()
+        self._check(self.L.ngrav_gpu_force_error(self.h, int(nsample), int(seed), int(fp64_pairs),
+                                                 ctypes.byref(f)), self.h)
+        return dict(rms=f.rms, max=f.max, median=f.median, nsample=f.nsample)
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.ngrav_gpu_get_stats(self.h, ctypes.byref(s)), self.h)
+        return s.as_dict()
+
+    def reset_cumulative(self):
+        self._check(self.L.ngrav_gpu_reset_cumulative(self.h), self.h)
+
+    def debug_tree(self):
+        nn = ctypes.c_int()
+        self._check(self.L.ngrav_gpu_debug_tree(self.h, ctypes.byref(nn), *([None] * 12)), self.h)
+        k, n = nn.value, self.n
+        t = dict(keys=np.zeros(n, np.uint64), order=np.zeros(n, np.int32), level=np.zeros(k, np.int32),
+                 prefix=np.zeros(k, np.uint64), count=np.zeros(k, np.int32), is_leaf=np.zeros(k, np.int32),
+                 center=np.zeros((k, 3)), half=np.zeros(k), com=np.zeros((k, 3)), mass=np.zeros(k),
+                 max_radius=np.zeros(k), quad=np.zeros((k, 5)))
+        self._check(self.L.ngrav_gpu_debug_tree(
+            self.h, ctypes.byref(nn), _p(t["keys"], _U64), _p(t["order"], _I), _p(t["level"], _I),
+            _p(t["prefix"], _U64), _p(t["count"], _I), _p(t["is_leaf"], _I), _p(t["center"], _D),
+            _p(t["half"], _D), _p(t["com"], _D), _p(t["mass"], _D), _p(t["max_radius"], _D),
+            _p(t["quad"], _D)), self.h)
+        return t
+
+
+def canonical(tree: dict) -> dict:
+    """Node rows sorted by (level, prefix) -- a numbering-independent topology."""
+    idx = np.lexsort((tree["prefix"], tree["level"]))
+    return {k: (v[idx] if k not in ("keys", "order") else v) for k, v in tree.items()}

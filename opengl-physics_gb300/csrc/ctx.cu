@@ -1,0 +1,779 @@
+// ctx.cu -- the C-ABI (include/ngrav_gpu.h): context, buffers, and the
+// host-side orchestration of one force evaluation / KDK step.
+//
+// One force evaluation enqueues, on the context's stream:
+//   reset counters -> bounding box + root cube -> 63-bit keys -> radix sort
+//   (8 passes) -> gather the state into key order -> tree levels 0..20 ->
+//   leaf list -> upward moments -> grouped walk (+ closing kick)
+// then synchronises once and reads the device status word.  A node-pool or
+// walk-stack overflow is reported by the kernels (never silently dropped, as
+// the reference's GL path does at GpuBarnesHut.cpp:259-260 and :428), the
+// walk refuses to run on a truncated tree, and the host grows the pool and
+// re-runs the evaluation.
+#include "ngrav_gpu.h"
+
+#include "ctx_kernels.cuh"
+#include "engine.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+using namespace ngrav;
+
+struct ngrav_gpu_ctx {
+    ngrav_gpu_opts opts{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    long long n = 0;
+    long long cap_n = 0;
+    Particles P;
+    SortBuffers SB;
+    NodeArrays T;
+    Counters* C = nullptr;
+    Counters hc{};
+    int* leaf_at = nullptr;
+    unsigned* flags = nullptr;
+    unsigned* scanbuf = nullptr;
+    int* leaf_list = nullptr;
+    int* stack_pool = nullptr;
+    int stack_cap = 0;
+    int nwarps = 0;
+    double* stage = nullptr;          // 7 * cap_n doubles (upload / download staging)
+    double* dpartial = nullptr;
+    long long dpartial_cap = 0;
+    int* inv = nullptr;
+    int* dtargets = nullptr;
+    int* dslots = nullptr;
+    double* dsamp = nullptr;
+    int samp_cap = 0;
+    bool have = false;
+    bool primed = false;
+    long long force_evals = 0;
+    cudaEvent_t ev[8] = {};
+    cudaEvent_t sev[2] = {};
+    bool events = false;
+    double phase_ms[7] = {};
+    // cumulative measurement counters (ngrav_gpu_reset_cumulative)
+    long long launches = 0;
+    long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
+    double cum_ms_walk = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
+};
+
+namespace {
+
+#define NG_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+            return (e_ == cudaErrorMemoryAllocation) ? NGRAV_ERR_OOM : NGRAV_ERR_CUDA;     \
+        }                                                                                  \
+    } while (0)
+
+#define NG_TRY(expr)          \
+    do {                      \
+        int rc_ = (expr);     \
+        if (rc_) return rc_;  \
+    } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+int fail(ngrav_gpu_ctx* ctx, int code, const std::string& msg) {
+    ctx->err = msg;
+    return code;
+}
+
+int check_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* o) {
+    if (!o) return fail(ctx, NGRAV_ERR_INVALID_ARG, "opts is NULL");
+    if (o->abi_version != NGRAV_GPU_ABI_VERSION) return fail(ctx, NGRAV_ERR_INVALID_ARG, "abi_version mismatch");
+    if (o->leaf_capacity < 1 || o->leaf_capacity > (1 << 20))
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "leaf_capacity out of range");
+    if (o->max_depth < 0) return fail(ctx, NGRAV_ERR_INVALID_ARG, "max_depth < 0");
+    if (!(o->theta >= 0.0) || !(o->eps >= 0.0) || !std::isfinite(o->G))
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "theta/eps/G invalid");
+    if (o->precision != NGRAV_PRECISION_PLAIN && o->precision != NGRAV_PRECISION_SPLIT)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "unknown precision");
+    if (o->mac != NGRAV_MAC_GEOMETRIC && o->mac != NGRAV_MAC_LEARNED)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "unknown mac");
+    return NGRAV_OK;
+}
+
+bool split_of(const ngrav_gpu_ctx* ctx) { return ctx->opts.precision == NGRAV_PRECISION_SPLIT; }
+
+void free_particles(ngrav_gpu_ctx* ctx) {
+    Particles& P = ctx->P;
+    dfree(P.pos); dfree(P.plo); dfree(P.vel); dfree(P.acc); dfree(P.src); dfree(P.id);
+    dfree(P.pos2); dfree(P.plo2); dfree(P.vel2); dfree(P.acc2); dfree(P.id2);
+    P.cap = 0;
+    SortBuffers& S = ctx->SB;
+    dfree(S.keys); dfree(S.keys_alt); dfree(S.vals); dfree(S.vals_alt); dfree(S.hist); dfree(S.scan_tmp);
+    S.cap = 0;
+    dfree(ctx->leaf_at); dfree(ctx->flags); dfree(ctx->scanbuf); dfree(ctx->leaf_list);
+    dfree(ctx->stage); dfree(ctx->inv);
+    ctx->cap_n = 0;
+}
+
+void free_nodes(ngrav_gpu_ctx* ctx) {
+    NodeArrays& T = ctx->T;
+    dfree(T.start); dfree(T.count); dfree(T.first_child); dfree(T.parent); dfree(T.visit);
+    dfree(T.nchild); dfree(T.level); dfree(T.cx); dfree(T.cy); dfree(T.cz);
+    dfree(T.mass); dfree(T.comx); dfree(T.comy); dfree(T.comz); dfree(T.maxr); dfree(T.quad);
+    dfree(T.wA); dfree(T.wB); dfree(T.wC); dfree(T.wD); dfree(T.chi); dfree(T.clo);
+    T.cap = 0;
+}
+
+template <typename T>
+cudaError_t dalloc(T*& p, long long count) {
+    return cudaMalloc((void**)&p, sizeof(T) * (size_t)(count > 0 ? count : 1));
+}
+
+int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
+    if (n <= ctx->cap_n) return NGRAV_OK;
+    free_particles(ctx);
+    const long long c = n;
+    Particles& P = ctx->P;
+    NG_CUDA(dalloc(P.pos, c)); NG_CUDA(dalloc(P.plo, c)); NG_CUDA(dalloc(P.vel, c)); NG_CUDA(dalloc(P.acc, c));
+    NG_CUDA(dalloc(P.src, c)); NG_CUDA(dalloc(P.id, c));
+    NG_CUDA(dalloc(P.pos2, c)); NG_CUDA(dalloc(P.plo2, c)); NG_CUDA(dalloc(P.vel2, c)); NG_CUDA(dalloc(P.acc2, c));
+    NG_CUDA(dalloc(P.id2, c));
+    P.cap = c;
+    SortBuffers& S = ctx->SB;
+    NG_CUDA(dalloc(S.keys, c)); NG_CUDA(dalloc(S.keys_alt, c)); NG_CUDA(dalloc(S.vals, c));
+    NG_CUDA(dalloc(S.vals_alt, c));
+    const long long nb = (c + 4095) / 4096;
+    S.hist_cap = nb * 256;
+    NG_CUDA(dalloc(S.hist, S.hist_cap));
+    S.scan_tmp_cap = scan_tmp_size(std::max(S.hist_cap, c)) + 16;
+    NG_CUDA(dalloc(S.scan_tmp, S.scan_tmp_cap));
+    S.cap = c;
+    NG_CUDA(dalloc(ctx->leaf_at, c)); NG_CUDA(dalloc(ctx->flags, c)); NG_CUDA(dalloc(ctx->scanbuf, c));
+    NG_CUDA(dalloc(ctx->leaf_list, c)); NG_CUDA(dalloc(ctx->inv, c));
+    NG_CUDA(dalloc(ctx->stage, 7 * c));
+    ctx->cap_n = c;
+    return NGRAV_OK;
+}
+
+int alloc_nodes(ngrav_gpu_ctx* ctx, int cap) {
+    free_nodes(ctx);
+    NodeArrays& T = ctx->T;
+    NG_CUDA(dalloc(T.start, cap)); NG_CUDA(dalloc(T.count, cap)); NG_CUDA(dalloc(T.first_child, cap));
+    NG_CUDA(dalloc(T.parent, cap)); NG_CUDA(dalloc(T.visit, cap)); NG_CUDA(dalloc(T.nchild, cap));
+    NG_CUDA(dalloc(T.level, cap)); NG_CUDA(dalloc(T.cx, cap)); NG_CUDA(dalloc(T.cy, cap)); NG_CUDA(dalloc(T.cz, cap));
+    NG_CUDA(dalloc(T.mass, cap)); NG_CUDA(dalloc(T.comx, cap)); NG_CUDA(dalloc(T.comy, cap));
+    NG_CUDA(dalloc(T.comz, cap)); NG_CUDA(dalloc(T.maxr, cap)); NG_CUDA(dalloc(T.quad, 5LL * cap));
+    NG_CUDA(dalloc(T.wA, cap)); NG_CUDA(dalloc(T.wB, cap)); NG_CUDA(dalloc(T.wC, cap)); NG_CUDA(dalloc(T.wD, cap));
+    NG_CUDA(dalloc(T.chi, cap)); NG_CUDA(dalloc(T.clo, cap));
+    T.cap = cap;
+    return NGRAV_OK;
+}
+
+int initial_node_cap(long long n, int leaf_cap) {
+    long long c = 5 * n / std::max(1, leaf_cap) + 1024;
+    c = std::min<long long>(c, 4 * n + 1024);
+    return (int)std::min<long long>(c, 0x7FFFFFF0LL);
+}
+
+int alloc_stack(ngrav_gpu_ctx* ctx, int stack_cap) {
+    dfree(ctx->stack_pool);
+    NG_CUDA(dalloc(ctx->stack_pool, (long long)ctx->nwarps * stack_cap));
+    ctx->stack_cap = stack_cap;
+    return NGRAV_OK;
+}
+
+WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
+    WalkParams wp{};
+    const ngrav_gpu_opts& o = ctx->opts;
+    wp.eps2 = (float)(o.eps * o.eps);
+    wp.eps2_d = o.eps * o.eps;
+    wp.theta = (float)o.theta;
+    wp.theta2 = (float)(o.theta * o.theta);
+    wp.theta2_d = o.theta * o.theta;
+    wp.G = (float)o.G;
+    wp.quadrupole = o.quadrupole ? 1 : 0;
+    wp.split = split_of(ctx) ? 1 : 0;
+    wp.retest = o.fp64_mac_retest ? 1 : 0;
+    wp.kick = kick ? 1 : 0;
+    wp.hdt = hdt;
+    wp.stack_cap = ctx->stack_cap;
+    wp.node_limit = ctx->T.cap + 32;
+    return wp;
+}
+
+void rec(ngrav_gpu_ctx* ctx, int i) {
+    if (ctx->events) cudaEventRecord(ctx->ev[i], ctx->stream);
+}
+
+// Enqueue one force evaluation. bbox_ready: the counters were reset and the
+// bounding box accumulated by the preceding kick-drift.
+void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
+    cudaStream_t s = ctx->stream;
+    const long long n = ctx->n;
+    const bool split = split_of(ctx);
+    Particles& P = ctx->P;
+    rec(ctx, 0);
+    if (!bbox_ready) {
+        launch_reset_counters(ctx->C, s);
+        launch_bbox(P.pos, split ? P.plo : nullptr, n, ctx->C, s);
+        ctx->launches += 2;
+    }
+    launch_root(ctx->C, n, s);
+    launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->SB.keys, ctx->SB.vals, s);
+    rec(ctx, 1);
+    const int passes = 8;
+    radix_sort_pairs(ctx->SB, n, passes, s);
+    launch_permute(P, ctx->SB.vals, n, split, s);
+    // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,
+    // tree init, 21 levels, leaf list (mark, 3 scan kernels, compact), moments, walk
+    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + kKeyLevels + 5 + 1 + 1;
+    std::swap(P.pos, P.pos2);
+    std::swap(P.plo, P.plo2);
+    std::swap(P.vel, P.vel2);
+    std::swap(P.acc, P.acc2);
+    std::swap(P.id, P.id2);
+    rec(ctx, 2);
+    launch_tree_init(ctx->T, ctx->C, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, s);
+    launch_tree_levels(ctx->T, ctx->C, ctx->SB.keys, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, s);
+    launch_leaf_list(ctx->T, ctx->C, n, ctx->leaf_at, ctx->flags, ctx->scanbuf, ctx->leaf_list, ctx->SB, s);
+    rec(ctx, 3);
+    launch_moments(ctx->T, ctx->C, P, ctx->leaf_list, n, (int)std::min<long long>(n, ctx->T.cap), split,
+                   ctx->opts.quadrupole != 0, s);
+    rec(ctx, 4);
+    launch_walk(ctx->T, ctx->C, P, ctx->leaf_list, (int)n, walk_params(ctx, kick, hdt), ctx->stack_pool,
+                ctx->nwarps, s);
+    rec(ctx, 5);
+}
+
+int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
+    retry = false;
+    NG_CUDA(cudaMemcpyAsync(&ctx->hc, ctx->C, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    NG_CUDA(cudaGetLastError());
+    const unsigned st = ctx->hc.status;
+    if (st & kStNonFinite) return fail(ctx, NGRAV_ERR_NONFINITE, "non-finite position or mass");
+    if (st & kStTimeout) return fail(ctx, NGRAV_ERR_TIMEOUT, "a bounded device wait ran out");
+    if (st & kStNodeOverflow) {
+        const long long want = std::min<long long>((long long)ctx->T.cap * 2, 0x7FFFFFF0LL);
+        if (want <= ctx->T.cap) return fail(ctx, NGRAV_ERR_CAPACITY, "node pool exhausted");
+        NG_TRY(alloc_nodes(ctx, (int)want));
+        retry = true;
+        return NGRAV_OK;
+    }
+    if (st & kStStackOverflow) {
+        if (ctx->stack_cap >= (1 << 22)) return fail(ctx, NGRAV_ERR_CAPACITY, "walk stack exhausted");
+        NG_TRY(alloc_stack(ctx, ctx->stack_cap * 2));
+        retry = true;
+        return NGRAV_OK;
+    }
+    if (ctx->opts.strict_depth && ctx->hc.depth_limited > 0)
+        return fail(ctx, NGRAV_ERR_DEPTH, "a leaf needs more than 21 key levels");
+    if (ctx->events) {
+        float ms;
+        for (int i = 0; i < 5; ++i) {
+            cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
+            ctx->phase_ms[i] = ms;
+        }
+        ctx->cum_ms_walk += ctx->phase_ms[4];
+        ctx->cum_ms_eval += ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] +
+                            ctx->phase_ms[4];
+    }
+    ctx->force_evals += 1;
+    ctx->cum_evals += 1;
+    ctx->cum_pairs += (long long)ctx->hc.p2p_pairs;
+    ctx->cum_p2c += (long long)ctx->hc.p2c_terms;
+    return NGRAV_OK;
+}
+
+int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        enqueue_eval(ctx, bbox_ready, kick, hdt);
+        bool retry = false;
+        NG_TRY(finish_eval(ctx, retry));
+        if (!retry) return NGRAV_OK;
+        bbox_ready = false;
+    }
+    return fail(ctx, NGRAV_ERR_CAPACITY, "capacity growth did not converge");
+}
+
+int ensure_samp(ngrav_gpu_ctx* ctx, int ns) {
+    if (ns <= ctx->samp_cap) return NGRAV_OK;
+    dfree(ctx->dtargets);
+    dfree(ctx->dslots);
+    dfree(ctx->dsamp);
+    NG_CUDA(dalloc(ctx->dtargets, ns));
+    NG_CUDA(dalloc(ctx->dslots, ns));
+    NG_CUDA(dalloc(ctx->dsamp, 3LL * ns));
+    ctx->samp_cap = ns;
+    return NGRAV_OK;
+}
+
+int ensure_partial(ngrav_gpu_ctx* ctx, long long count) {
+    if (count <= ctx->dpartial_cap) return NGRAV_OK;
+    dfree(ctx->dpartial);
+    NG_CUDA(dalloc(ctx->dpartial, count));
+    ctx->dpartial_cap = count;
+    return NGRAV_OK;
+}
+
+template <typename T>
+int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, const T* z, const T* vx, const T* vy,
+                       const T* vz, const T* m, bool f64) {
+    if (n < 0 || n > 0x7FFFFFF0LL) return fail(ctx, NGRAV_ERR_INVALID_ARG, "n out of range");
+    if (n > 0 && (!x || !y || !z || !m)) return fail(ctx, NGRAV_ERR_INVALID_ARG, "NULL position/mass array");
+    const bool have_v = vx && vy && vz;
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    NG_TRY(alloc_particles(ctx, std::max<int64_t>(n, 1)));
+    if (ctx->T.cap < initial_node_cap(n, ctx->opts.leaf_capacity))
+        NG_TRY(alloc_nodes(ctx, initial_node_cap(n, ctx->opts.leaf_capacity)));
+    ctx->n = n;
+    if (n > 0) {
+        T* st = reinterpret_cast<T*>(ctx->stage);
+        const size_t b = sizeof(T) * (size_t)n;
+        const T* srcs[7] = {x, y, z, vx, vy, vz, m};
+        for (int k = 0; k < 7; ++k) {
+            if (!srcs[k]) continue;
+            NG_CUDA(cudaMemcpyAsync(st + (size_t)k * n, srcs[k], b, cudaMemcpyHostToDevice, ctx->stream));
+        }
+        const T* dv[3] = {have_v ? st + 3 * (size_t)n : nullptr, have_v ? st + 4 * (size_t)n : nullptr,
+                          have_v ? st + 5 * (size_t)n : nullptr};
+        if (f64)
+            launch_upload_f64(n, (const double*)st, (const double*)(st + n), (const double*)(st + 2 * n),
+                              (const double*)dv[0], (const double*)dv[1], (const double*)dv[2],
+                              (const double*)(st + 6 * n), ctx->P, split_of(ctx), ctx->stream);
+        else
+            launch_upload_f32(n, (const float*)st, (const float*)(st + n), (const float*)(st + 2 * n),
+                              (const float*)dv[0], (const float*)dv[1], (const float*)dv[2],
+                              (const float*)(st + 6 * n), ctx->P, split_of(ctx), ctx->stream);
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        NG_CUDA(cudaGetLastError());
+    }
+    ctx->have = n > 0;
+    ctx->primed = false;
+    return NGRAV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ngrav_gpu_default_opts(ngrav_gpu_opts* o) {
+    if (!o) return NGRAV_ERR_INVALID_ARG;
+    std::memset(o, 0, sizeof(*o));
+    o->abi_version = NGRAV_GPU_ABI_VERSION;
+    o->device = 0;
+    o->leaf_capacity = 8;
+    o->max_depth = 40;
+    o->quadrupole = 1;
+    o->mac = NGRAV_MAC_GEOMETRIC;
+    o->precision = NGRAV_PRECISION_SPLIT;
+    o->fp64_mac_retest = 1;
+    o->strict_depth = 0;
+    o->timing = 0;
+    o->G = 1.0;
+    o->eps = 0.05;
+    o->theta = 0.5;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_create(ngrav_gpu_ctx** out, const ngrav_gpu_opts* opts) {
+    if (!out) return NGRAV_ERR_INVALID_ARG;
+    *out = nullptr;
+    ngrav_gpu_ctx* ctx = new (std::nothrow) ngrav_gpu_ctx();
+    if (!ctx) return NGRAV_ERR_OOM;
+    int rc = check_opts(ctx, opts);
+    if (rc) {
+        delete ctx;
+        return rc;
+    }
+    ctx->opts = *opts;
+    auto init = [&]() -> int {
+        NG_CUDA(cudaSetDevice(ctx->opts.device));
+        NG_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->opts.device));
+        NG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        NG_CUDA(cudaMalloc((void**)&ctx->C, sizeof(Counters)));
+        walk_set_attributes();
+        NG_CUDA(cudaGetLastError());
+        ctx->nwarps = ctx->sm_count * walk_blocks_per_sm() * walk_warps_per_block();
+        NG_TRY(alloc_stack(ctx, 4096));
+        for (int i = 0; i < 8; ++i) NG_CUDA(cudaEventCreate(&ctx->ev[i]));
+        for (int i = 0; i < 2; ++i) NG_CUDA(cudaEventCreate(&ctx->sev[i]));
+        ctx->events = ctx->opts.timing != 0;
+        return NGRAV_OK;
+    };
+    rc = init();
+    if (rc) {
+        // keep the message reachable only through the return code
+        ngrav_gpu_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return NGRAV_OK;
+}
+
+void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->opts.device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_particles(ctx);
+    free_nodes(ctx);
+    dfree(ctx->C);
+    dfree(ctx->stack_pool);
+    dfree(ctx->dpartial);
+    dfree(ctx->dtargets);
+    dfree(ctx->dslots);
+    dfree(ctx->dsamp);
+    for (int i = 0; i < 8; ++i)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < 2; ++i)
+        if (ctx->sev[i]) cudaEventDestroy(ctx->sev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* ngrav_gpu_last_error(const ngrav_gpu_ctx* ctx) {
+    if (!ctx) return "NULL context";
+    return ctx->err.c_str();
+}
+
+int ngrav_gpu_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* opts) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    NG_TRY(check_opts(ctx, opts));
+    if (opts->device != ctx->opts.device) return fail(ctx, NGRAV_ERR_INVALID_ARG, "device cannot change");
+    const bool prec_change = opts->precision != ctx->opts.precision;
+    if (prec_change && ctx->have) {
+        // PLAIN -> SPLIT starts with lo = 0; SPLIT -> PLAIN rounds hi + lo to FP32.
+        NG_CUDA(cudaSetDevice(ctx->opts.device));
+        if (opts->precision == NGRAV_PRECISION_SPLIT)
+            NG_CUDA(cudaMemsetAsync(ctx->P.plo, 0, sizeof(float4) * ctx->n, ctx->stream));
+        else
+            launch_collapse_split(ctx->P.pos, ctx->P.plo, ctx->n, ctx->stream);
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->opts = *opts;
+    ctx->events = ctx->opts.timing != 0;
+    ctx->primed = false;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, const double* y, const double* z,
+                            const double* vx, const double* vy, const double* vz, const double* m) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    return set_particles_impl<double>(ctx, n, x, y, z, vx, vy, vz, m, true);
+}
+
+int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
+                                const float* vx, const float* vy, const float* vz, const float* m) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    return set_particles_impl<float>(ctx, n, x, y, z, vx, vy, vz, m, false);
+}
+
+int ngrav_gpu_compute_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!ax || !ay || !az) return fail(ctx, NGRAV_ERR_INVALID_ARG, "NULL output array");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    NG_TRY(evaluate(ctx, false, false, 0.f));
+    ctx->primed = true;
+    const long long n = ctx->n;
+    double* st = ctx->stage;
+    launch_download(n, ctx->P.id, ctx->P.acc, nullptr, st, st + n, st + 2 * n, ctx->stream);
+    NG_CUDA(cudaMemcpyAsync(ax, st, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaMemcpyAsync(ay, st + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaMemcpyAsync(az, st + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_prime(ngrav_gpu_ctx* ctx) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    NG_TRY(evaluate(ctx, false, false, 0.f));
+    ctx->primed = true;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_step(ngrav_gpu_ctx* ctx, int nsteps, double dt) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (nsteps < 0 || !std::isfinite(dt)) return fail(ctx, NGRAV_ERR_INVALID_ARG, "bad nsteps/dt");
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    if (!ctx->primed) NG_TRY(ngrav_gpu_prime(ctx));
+    const float hdt = (float)(0.5 * dt), fdt = (float)dt;
+    NG_CUDA(cudaEventRecord(ctx->sev[0], ctx->stream));
+    for (int k = 0; k < nsteps; ++k) {
+        launch_reset_counters(ctx->C, ctx->stream);
+        launch_kick_drift(ctx->P, ctx->n, hdt, fdt, split_of(ctx), ctx->C, ctx->stream);
+        ctx->launches += 2;
+        NG_TRY(evaluate(ctx, true, true, hdt));
+    }
+    NG_CUDA(cudaEventRecord(ctx->sev[1], ctx->stream));
+    NG_CUDA(cudaEventSynchronize(ctx->sev[1]));
+    float ms = 0.f;
+    NG_CUDA(cudaEventElapsedTime(&ms, ctx->sev[0], ctx->sev[1]));
+    ctx->cum_ms_step += ms;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, double* vx, double* vy, double* vz) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    double* st = ctx->stage;
+    launch_download(n, ctx->P.id, ctx->P.pos, split_of(ctx) ? ctx->P.plo : nullptr, st, st + n, st + 2 * n,
+                    ctx->stream);
+    launch_download(n, ctx->P.id, ctx->P.vel, nullptr, st + 3 * n, st + 4 * n, st + 5 * n, ctx->stream);
+    double* outs[6] = {x, y, z, vx, vy, vz};
+    for (int k = 0; k < 6; ++k)
+        if (outs[k])
+            NG_CUDA(cudaMemcpyAsync(outs[k], st + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_get_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    double* st = ctx->stage;
+    launch_download(n, ctx->P.id, ctx->P.acc, nullptr, st, st + n, st + 2 * n, ctx->stream);
+    double* outs[3] = {ax, ay, az};
+    for (int k = 0; k < 3; ++k)
+        if (outs[k])
+            NG_CUDA(cudaMemcpyAsync(outs[k], st + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_diag* out) {
+    if (!ctx || !out) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    const bool split = split_of(ctx);
+    const int nb = diag_blocks(n);
+    const int npb = potential_blocks(n);
+    NG_TRY(ensure_partial(ctx, std::max<long long>(8LL * nb, npb) + 8));
+    std::vector<double> h(std::max<long long>(8LL * nb, npb));
+    launch_diag_pass1(n, ctx->P, split, ctx->dpartial, ctx->stream);
+    NG_CUDA(cudaMemcpyAsync(h.data(), ctx->dpartial, sizeof(double) * 8 * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double s1[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < 8; ++k) s1[k] += h[8 * b + k];
+    const double M = s1[0];
+    double com[3] = {s1[1], s1[2], s1[3]};
+    if (M > 0.0)
+        for (double& c : com) c /= M;
+    launch_diag_pass2(n, ctx->P, split, com[0], com[1], com[2], ctx->dpartial, ctx->stream);
+    NG_CUDA(cudaMemcpyAsync(h.data(), ctx->dpartial, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double L[3] = {0, 0, 0};
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < 3; ++k) L[k] += h[3 * b + k];
+    out->kinetic = s1[4];
+    for (int k = 0; k < 3; ++k) {
+        out->com[k] = com[k];
+        out->L[k] = L[k];
+        out->P[k] = s1[5 + k];
+    }
+    const bool exact = exact_potential || n <= 262144;
+    out->potential_exact = exact ? 1 : 0;
+    if (exact) {
+        launch_potential(n, ctx->P, split, ctx->opts.eps * ctx->opts.eps, ctx->dpartial, ctx->stream);
+        NG_CUDA(cudaMemcpyAsync(h.data(), ctx->dpartial, sizeof(double) * npb, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        double pot = 0.0;
+        for (int b = 0; b < npb; ++b) pot += h[b];
+        out->potential = ctx->opts.G * pot;
+    } else {
+        out->potential = std::nan("");
+    }
+    out->energy = out->kinetic + out->potential;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp64_pairs, ngrav_gpu_ferr* out) {
+    if (!ctx || !out) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    const long long n = ctx->n;
+    if (nsample <= 0 || nsample > n) return fail(ctx, NGRAV_ERR_INVALID_ARG, "nsample out of range");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    // Floyd's sampling without replacement, splitmix64 stream.
+    uint64_t st = seed;
+    auto next = [&st]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    std::unordered_set<long long> chosen;
+    std::vector<int> targets;
+    targets.reserve(nsample);
+    for (long long j = n - nsample; j < n; ++j) {
+        const long long t = (long long)(next() % (uint64_t)(j + 1));
+        const long long pick = chosen.count(t) ? j : t;
+        chosen.insert(pick);
+        targets.push_back((int)pick);
+    }
+    std::sort(targets.begin(), targets.end());
+    NG_TRY(ensure_samp(ctx, nsample));
+    NG_CUDA(cudaMemcpyAsync(ctx->dtargets, targets.data(), sizeof(int) * nsample, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    launch_inverse_id(n, ctx->P.id, ctx->inv, ctx->stream);
+    launch_gather_slots(ctx->inv, ctx->dtargets, nsample, ctx->dslots, ctx->stream);
+    launch_sampler(n, ctx->P, split_of(ctx), ctx->dslots, nsample, ctx->opts.eps * ctx->opts.eps, fp64_pairs != 0,
+                   ctx->dsamp, ctx->stream);
+    std::vector<double> ref(3 * (size_t)nsample);
+    std::vector<int> slots(nsample);
+    NG_CUDA(cudaMemcpyAsync(ref.data(), ctx->dsamp, sizeof(double) * 3 * nsample, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    NG_CUDA(cudaMemcpyAsync(slots.data(), ctx->dslots, sizeof(int) * nsample, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    NG_CUDA(cudaGetLastError());
+    std::vector<float4> acc(nsample);
+    for (int k = 0; k < nsample; ++k)
+        NG_CUDA(cudaMemcpyAsync(&acc[k], ctx->P.acc + slots[k], sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> rel(nsample);
+    double s2 = 0.0, mx = 0.0;
+    for (int k = 0; k < nsample; ++k) {
+        const double G = ctx->opts.G;
+        const double rx = G * ref[3 * k], ry = G * ref[3 * k + 1], rz = G * ref[3 * k + 2];
+        const double ex = acc[k].x - rx, ey = acc[k].y - ry, ez = acc[k].z - rz;
+        const double r = std::sqrt(ex * ex + ey * ey + ez * ez) /
+                         std::max(std::sqrt(rx * rx + ry * ry + rz * rz), 1e-30);
+        rel[k] = r;
+        s2 += r * r;
+        mx = std::max(mx, r);
+    }
+    std::sort(rel.begin(), rel.end());
+    out->rms = std::sqrt(s2 / nsample);
+    out->max = mx;
+    out->median = (nsample & 1) ? rel[nsample / 2] : 0.5 * (rel[nsample / 2 - 1] + rel[nsample / 2]);
+    out->nsample = nsample;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
+    if (!ctx || !out) return NGRAV_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    const Counters& c = ctx->hc;
+    out->ms_bbox_keys = ctx->phase_ms[0];
+    out->ms_sort = ctx->phase_ms[1];
+    out->ms_build = ctx->phase_ms[2];
+    out->ms_moments = ctx->phase_ms[3];
+    out->ms_walk = ctx->phase_ms[4];
+    out->ms_total = ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] + ctx->phase_ms[4];
+    out->p2p_pairs = (long long)c.p2p_pairs;
+    out->p2c_terms = (long long)c.p2c_terms;
+    out->mac_tests = (long long)c.mac_tests;
+    out->mac_retests = (long long)c.mac_retests;
+    out->groups = (long long)c.groups;
+    out->nodes = std::min(c.next_free, ctx->T.cap);
+    out->leaves = c.nleaves;
+    out->levels = c.levels_used;
+    out->max_leaf_count = c.max_leaf_count;
+    out->depth_limited_leaves = c.depth_limited;
+    out->walk_stack_max = c.stack_max;
+    out->status_bits = c.status;
+    out->force_evals = ctx->force_evals;
+    out->n = ctx->n;
+    out->cum_evals = ctx->cum_evals;
+    out->cum_p2p_pairs = ctx->cum_pairs;
+    out->cum_p2c_terms = ctx->cum_p2c;
+    out->cum_ms_walk = ctx->cum_ms_walk;
+    out->cum_ms_eval = ctx->cum_ms_eval;
+    out->cum_ms_step = ctx->cum_ms_step;
+    out->cum_launches = ctx->launches;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_reset_cumulative(ngrav_gpu_ctx* ctx) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    ctx->launches = 0;
+    ctx->cum_evals = ctx->cum_pairs = ctx->cum_p2c = 0;
+    ctx->cum_ms_walk = ctx->cum_ms_eval = ctx->cum_ms_step = 0.0;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_probe_fp32_peak(int device, double* tflops) {
+    if (!tflops) return NGRAV_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return NGRAV_ERR_CUDA;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return NGRAV_ERR_CUDA;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return NGRAV_ERR_CUDA;
+    *tflops = run_fma_probe(sms, s);
+    cudaStreamDestroy(s);
+    return *tflops > 0.0 ? NGRAV_OK : NGRAV_ERR_CUDA;
+}
+
+int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* order, int* level, uint64_t* prefix,
+                         int* count, int* is_leaf, double* center, double* half, double* com, double* mass,
+                         double* max_radius, double* quad) {
+    if (!ctx || !nnodes) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have || ctx->force_evals == 0) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no tree built yet");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const int nn = std::min(ctx->hc.next_free, ctx->T.cap);
+    *nnodes = nn;
+    if (!keys && !order && !level) return NGRAV_OK;
+    const long long n = ctx->n;
+    std::vector<unsigned long long> hk(n);
+    std::vector<int> id(n);
+    NG_CUDA(cudaMemcpy(hk.data(), ctx->SB.keys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    NG_CUDA(cudaMemcpy(id.data(), ctx->P.id, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (keys)
+        for (long long k = 0; k < n; ++k) keys[id[k]] = hk[k];
+    std::vector<int> st(nn), ct(nn), fc(nn);
+    std::vector<unsigned char> lv(nn);
+    NG_CUDA(cudaMemcpy(st.data(), ctx->T.start, sizeof(int) * nn, cudaMemcpyDeviceToHost));
+    NG_CUDA(cudaMemcpy(ct.data(), ctx->T.count, sizeof(int) * nn, cudaMemcpyDeviceToHost));
+    NG_CUDA(cudaMemcpy(fc.data(), ctx->T.first_child, sizeof(int) * nn, cudaMemcpyDeviceToHost));
+    NG_CUDA(cudaMemcpy(lv.data(), ctx->T.level, nn, cudaMemcpyDeviceToHost));
+    if (order) {
+        // Leaves partition [0, n) in key order; within a leaf the reference
+        // lists members in ascending original index (Tree.cpp:130-133, :169).
+        for (long long k = 0; k < n; ++k) order[k] = id[k];
+        for (int v = 0; v < nn; ++v)
+            if (fc[v] == -1) std::sort(order + st[v], order + st[v] + ct[v]);
+    }
+    const double h0 = ctx->hc.root_half;
+    std::vector<double> tmp(nn);
+    for (int v = 0; v < nn; ++v) {
+        if (level) level[v] = lv[v];
+        if (prefix) prefix[v] = lv[v] == 0 ? 0ull : (hk[st[v]] >> (3 * (kKeyLevels - lv[v])));
+        if (count) count[v] = ct[v];
+        if (is_leaf) is_leaf[v] = fc[v] == -1;
+        if (half) half[v] = std::ldexp(h0, -(int)lv[v]);
+    }
+    auto get3 = [&](double* dst, const double* a, const double* b, const double* c) -> int {
+        if (!dst) return NGRAV_OK;
+        const double* src[3] = {a, b, c};
+        for (int k = 0; k < 3; ++k) {
+            NG_CUDA(cudaMemcpy(tmp.data(), src[k], sizeof(double) * nn, cudaMemcpyDeviceToHost));
+            for (int v = 0; v < nn; ++v) dst[3 * v + k] = tmp[v];
+        }
+        return NGRAV_OK;
+    };
+    NG_TRY(get3(center, ctx->T.cx, ctx->T.cy, ctx->T.cz));
+    NG_TRY(get3(com, ctx->T.comx, ctx->T.comy, ctx->T.comz));
+    if (mass) NG_CUDA(cudaMemcpy(mass, ctx->T.mass, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    if (max_radius) NG_CUDA(cudaMemcpy(max_radius, ctx->T.maxr, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    if (quad) NG_CUDA(cudaMemcpy(quad, ctx->T.quad, sizeof(double) * 5 * nn, cudaMemcpyDeviceToHost));
+    return NGRAV_OK;
+}
+
+}  // extern "C"

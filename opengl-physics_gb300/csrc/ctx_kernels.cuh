@@ -1,0 +1,34 @@
+// ctx_kernels.cuh -- launchers of kdk.cu used by the context (internal).
+#pragma once
+
+#include "engine.cuh"
+
+namespace ngrav {
+
+void launch_upload_f64(long long n, const double* x, const double* y, const double* z, const double* vx,
+                       const double* vy, const double* vz, const double* m, const Particles& P, bool split,
+                       cudaStream_t s);
+void launch_upload_f32(long long n, const float* x, const float* y, const float* z, const float* vx,
+                       const float* vy, const float* vz, const float* m, const Particles& P, bool split,
+                       cudaStream_t s);
+void launch_download(long long n, const int* id, const float4* a, const float4* alo, double* ox, double* oy,
+                     double* oz, cudaStream_t s);
+void launch_inverse_id(long long n, const int* id, int* inv, cudaStream_t s);
+int diag_blocks(long long n);
+void launch_diag_pass1(long long n, const Particles& P, bool split, double* partial, cudaStream_t s);
+void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, double cy, double cz, double* partial,
+                       cudaStream_t s);
+int potential_blocks(long long n);
+void launch_potential(long long n, const Particles& P, bool split, double eps2, double* partial, cudaStream_t s);
+void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
+                    bool fp64_pairs, double* out, cudaStream_t s);
+void launch_reset_counters(Counters* C, cudaStream_t s);
+int walk_blocks_for(int nwarps);
+size_t walk_smem_bytes();
+void walk_set_attributes();
+int walk_warps_per_block();
+int walk_blocks_per_sm();
+void launch_gather_slots(const int* inv, const int* targets, int nt, int* slots, cudaStream_t s);
+double run_fma_probe(int sm_count, cudaStream_t s);
+
+}  // namespace ngrav

@@ -1,0 +1,164 @@
+// engine.cuh -- device data layout and kernel launchers of the GB300
+// Barnes-Hut engine (internal; the public surface is include/ngrav_gpu.h).
+//
+// Layout in HBM (all particle arrays in the current tree order, i.e. sorted
+// by 63-bit octant-path key; `id` maps a slot back to the caller's index):
+//   pos   float4 (x_hi, y_hi, z_hi, m)     the state (FP32, or the high half)
+//   plo   float4 (x_lo, y_lo, z_lo, 0)     low half of double-float positions (SPLIT)
+//   vel   float4 (vx, vy, vz, 0)
+//   acc   float4 (ax, ay, az, 0)           G included
+//   src   float4 (ox, oy, oz, m)           walk input: offset from the own leaf's
+//                                           centre (SPLIT) or absolute (PLAIN)
+//   id    int
+// Nodes (one record per node, breadth-first by level; children of a node are
+// contiguous and in ascending octant order):
+//   start/count/first_child/parent/level/nchild, centre (FP64), FP64 moments,
+//   and four float4 walk records (see NodeWalk below).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ngrav {
+
+constexpr int kKeyLevels = 21;          // 63-bit keys: 3 bits per level
+constexpr int kMaxLevels = kKeyLevels + 1;
+
+// Device status word bits (sticky within one force evaluation).
+enum : unsigned {
+    kStNodeOverflow = 1u,
+    kStStackOverflow = 2u,
+    kStDepthLimit = 4u,     // warning: a depth-21 leaf holds more than leaf_capacity
+    kStNonFinite = 8u,
+    kStTimeout = 16u,
+    kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout,
+};
+
+// Per-evaluation device counters (zeroed before each force evaluation).
+struct Counters {
+    unsigned long long p2p_pairs;
+    unsigned long long p2c_terms;
+    unsigned long long mac_tests;
+    unsigned long long mac_retests;
+    unsigned long long groups;
+    unsigned long long bbox_min[3];   // order-preserving encoded FP64
+    unsigned long long bbox_max[3];
+    unsigned status;
+    int next_free;                    // node allocator
+    int level_begin[kMaxLevels + 2];
+    int done_blocks;
+    int nleaves;
+    int max_leaf_count;
+    int depth_limited;
+    int work_next;                    // dynamic group scheduler
+    int stack_max;
+    int levels_used;
+    int pad;
+    double root_center[3];
+    double root_half;
+};
+
+struct NodeArrays {
+    int cap = 0;
+    int* start = nullptr;
+    int* count = nullptr;
+    int* first_child = nullptr;       // -1 for leaves
+    int* parent = nullptr;
+    int* visit = nullptr;             // upward-pass arrival counters
+    unsigned char* nchild = nullptr;
+    unsigned char* level = nullptr;
+    double* cx = nullptr;             // geometric centre (FP64 recurrence of the reference)
+    double* cy = nullptr;
+    double* cz = nullptr;
+    // FP64 moments
+    double* mass = nullptr;
+    double* comx = nullptr;
+    double* comy = nullptr;
+    double* comz = nullptr;
+    double* maxr = nullptr;
+    double* quad = nullptr;           // 5 per node
+    // FP32 walk records
+    float4* wA = nullptr;             // com_hi.xyz, mass
+    float4* wB = nullptr;             // Qxx, Qyy, Qxy, Qxz
+    float4* wC = nullptr;             // Qyz, 2h, link (int bits), meta (int bits)
+    float4* wD = nullptr;             // com_lo.xyz, maxR (leaves, rounded up)
+    float4* chi = nullptr;            // centre hi (leaves; SPLIT)
+    float4* clo = nullptr;            // centre lo (leaves; SPLIT)
+};
+
+// wC.w meta: bit 31 leaf flag; bits 0..23 count (leaf) or nchild (internal);
+// bits 24..28 level.
+__host__ __device__ inline int meta_pack(bool leaf, int count_or_nchild, int level) {
+    return (leaf ? (int)0x80000000u : 0) | ((level & 31) << 24) | (count_or_nchild & 0xFFFFFF);
+}
+
+struct Particles {
+    long long cap = 0;
+    float4* pos = nullptr;
+    float4* plo = nullptr;
+    float4* vel = nullptr;
+    float4* acc = nullptr;
+    float4* src = nullptr;
+    int* id = nullptr;
+    // ping-pong partners for the permutation
+    float4* pos2 = nullptr;
+    float4* plo2 = nullptr;
+    float4* vel2 = nullptr;
+    float4* acc2 = nullptr;
+    int* id2 = nullptr;
+};
+
+struct SortBuffers {
+    long long cap = 0;
+    unsigned long long* keys = nullptr;
+    unsigned long long* keys_alt = nullptr;
+    unsigned* vals = nullptr;
+    unsigned* vals_alt = nullptr;
+    unsigned* hist = nullptr;         // 256 x blocks
+    unsigned* scan_tmp = nullptr;
+    long long hist_cap = 0;
+    long long scan_tmp_cap = 0;
+};
+
+struct WalkParams {
+    float eps2;
+    float theta;
+    float theta2;
+    float G;
+    double theta2_d;
+    double eps2_d;
+    int quadrupole;
+    int split;
+    int retest;
+    int kick;                         // apply closing half-kick v += hdt * a
+    float hdt;
+    int stack_cap;
+    int node_limit;                   // visits per group beyond this mean a corrupt tree
+};
+
+// ---- launchers (each enqueues on `s`; no host synchronisation) ----
+void launch_bbox(const float4* pos, const float4* plo, long long n, Counters* C, cudaStream_t s);
+void launch_root(Counters* C, long long n, cudaStream_t s);
+void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s);
+void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, unsigned long long* keys,
+                 unsigned* vals, cudaStream_t s);
+// Stable LSD radix sort of (keys, vals) over bits [0, 8*passes); result ends
+// in (keys, vals) (the alternates are scratch).
+void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s);
+void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);
+void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s);
+void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
+                        int max_depth, cudaStream_t s);
+void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, unsigned* flags, unsigned* scan_out,
+                      int* leaf_list, SortBuffers& sb, cudaStream_t s);
+void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,
+                    int max_leaves, bool split, bool quadrupole, cudaStream_t s);
+void launch_walk(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, int max_leaves,
+                 const WalkParams& wp, int* stack_pool, int nwarps, cudaStream_t s);
+void launch_kick_drift(const Particles& P, long long n, float hdt, float dt, bool split, Counters* C,
+                       cudaStream_t s);
+void launch_scatter_accel(const Particles& P, long long n, double* ax, double* ay, double* az, cudaStream_t s);
+void device_exclusive_scan(const unsigned* in, unsigned* out, long long n, unsigned* tmp, cudaStream_t s);
+long long scan_tmp_size(long long n);
+
+}  // namespace ngrav

@@ -1,0 +1,495 @@
+// kdk.cu -- state upload/download, the fused opening kick + drift, FP64
+// conservation diagnostics and the direct-sum force-error sampler.
+//
+// KDK (restating projects/nbody_core/src/Integrator.cpp:9-39):
+//   v += dt/2 a;  x += dt v;  a = F(x);  v += dt/2 a.
+// The first two updates are one streaming kernel here (kick_drift_kernel);
+// the closing kick is fused into the walk's epilogue.  In SPLIT precision the
+// drift adds dt*v to a double-float (hi, lo) position with an error-free
+// two-sum, so the state keeps ~48 significant bits.
+//
+// Diagnostics (restating include/ngrav/System.hpp:119-193 and
+// src/DeckSim.cpp:147-153): kinetic energy, centre of mass, angular momentum
+// about the COM and linear momentum are FP64 block reductions combined in a
+// fixed order (deterministic); the potential is the exact FP64 pair sum
+// sum_{i<j} -G m_i m_j / sqrt(r^2 + eps^2).
+#include "engine.cuh"
+#include "ctx_kernels.cuh"
+
+namespace ngrav {
+
+__device__ __forceinline__ unsigned long long enc_f64_k(double d) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// ---------------------------------------------------------------------------
+// Upload / download
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void upload_kernel(long long n, const T* __restrict__ x, const T* __restrict__ y,
+                              const T* __restrict__ z, const T* __restrict__ vx, const T* __restrict__ vy,
+                              const T* __restrict__ vz, const T* __restrict__ m, Particles P, int split) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double dx = (double)x[i], dy = (double)y[i], dz = (double)z[i];
+        const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+        P.pos[i] = make_float4(hx, hy, hz, (float)m[i]);
+        if (split) P.plo[i] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
+        P.vel[i] = vx ? make_float4((float)vx[i], (float)vy[i], (float)vz[i], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        P.acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        P.id[i] = (int)i;
+    }
+}
+
+static unsigned grid_for(long long n, int threads, int max_blocks) {
+    long long b = (n + threads - 1) / threads;
+    if (b > max_blocks) b = max_blocks;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+void launch_upload_f64(long long n, const double* x, const double* y, const double* z, const double* vx,
+                       const double* vy, const double* vz, const double* m, const Particles& P, bool split,
+                       cudaStream_t s) {
+    upload_kernel<double><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, x, y, z, vx, vy, vz, m, P, split ? 1 : 0);
+}
+
+void launch_upload_f32(long long n, const float* x, const float* y, const float* z, const float* vx,
+                       const float* vy, const float* vz, const float* m, const Particles& P, bool split,
+                       cudaStream_t s) {
+    upload_kernel<float><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, x, y, z, vx, vy, vz, m, P, split ? 1 : 0);
+}
+
+// out[id[k]] = value of slot k, as FP64, for positions (hi + lo), velocities
+// or accelerations.
+__global__ void download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ a,
+                                const float4* __restrict__ alo, double* __restrict__ ox, double* __restrict__ oy,
+                                double* __restrict__ oz) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const float4 v = a[k];
+        double x = v.x, y = v.y, z = v.z;
+        if (alo) {
+            const float4 l = alo[k];
+            x += (double)l.x;
+            y += (double)l.y;
+            z += (double)l.z;
+        }
+        const int i = id[k];
+        ox[i] = x;
+        oy[i] = y;
+        oz[i] = z;
+    }
+}
+
+void launch_download(long long n, const int* id, const float4* a, const float4* alo, double* ox, double* oy,
+                     double* oz, cudaStream_t s) {
+    download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, a, alo, ox, oy, oz);
+}
+
+__global__ void inverse_id_kernel(long long n, const int* __restrict__ id, int* __restrict__ inv) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        inv[id[k]] = (int)k;
+}
+
+void launch_inverse_id(long long n, const int* id, int* inv, cudaStream_t s) {
+    inverse_id_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, inv);
+}
+
+__global__ void gather_slots_kernel(const int* __restrict__ inv, const int* __restrict__ targets, int nt,
+                                    int* __restrict__ slots) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nt) slots[k] = inv[targets[k]];
+}
+
+void launch_gather_slots(const int* inv, const int* targets, int nt, int* slots, cudaStream_t s) {
+    if (nt > 0) gather_slots_kernel<<<(nt + 255) / 256, 256, 0, s>>>(inv, targets, nt, slots);
+}
+
+// ---------------------------------------------------------------------------
+// Opening kick + drift (+ the bounding box of the drifted positions)
+// ---------------------------------------------------------------------------
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(256) kick_drift_kernel(long long n, float4* __restrict__ pos,
+                                                         float4* __restrict__ plo, float4* __restrict__ vel,
+                                                         const float4* __restrict__ acc, float hdt, float dt,
+                                                         Counters* C) {
+    double lo[3] = {1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0};
+    double hi[3] = {-1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0};
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 v = vel[i];
+        const float4 a = acc[i];
+        v.x = fmaf(hdt, a.x, v.x);
+        v.y = fmaf(hdt, a.y, v.y);
+        v.z = fmaf(hdt, a.z, v.z);
+        vel[i] = v;
+        float4 p = pos[i];
+        double q[3];
+        if (SPLIT) {
+            float4 l = plo[i];
+            float* ph = &p.x;
+            float* pl = &l.x;
+            const float dv[3] = {dt * v.x, dt * v.y, dt * v.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                // two-sum of hi + d, error folded into lo, then renormalised
+                const float s = ph[k] + dv[k];
+                const float bb = s - ph[k];
+                const float e = (ph[k] - (s - bb)) + (dv[k] - bb);
+                const float lo2 = pl[k] + e;
+                const float h2 = s + lo2;
+                pl[k] = lo2 - (h2 - s);
+                ph[k] = h2;
+                q[k] = (double)ph[k] + (double)pl[k];
+            }
+            plo[i] = l;
+        } else {
+            p.x = fmaf(dt, v.x, p.x);
+            p.y = fmaf(dt, v.y, p.y);
+            p.z = fmaf(dt, v.z, p.z);
+            q[0] = p.x;
+            q[1] = p.y;
+            q[2] = p.z;
+        }
+        pos[i] = p;
+        bad |= !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fmin(lo[k], q[k]);
+            hi[k] = fmax(hi[k], q[k]);
+        }
+    }
+    __shared__ double slo[3][8], shi[3][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double l = lo[k], h = hi[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if (lane == 0) {
+            slo[k][w] = l;
+            shi[k][w] = h;
+        }
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        double l = slo[k][0], h = shi[k][0];
+        for (int j = 1; j < 8; ++j) {
+            l = fmin(l, slo[k][j]);
+            h = fmax(h, shi[k][j]);
+        }
+        atomicMin(&C->bbox_min[k], enc_f64_k(l));
+        atomicMax(&C->bbox_max[k], enc_f64_k(h));
+    }
+    if (threadIdx.x == 0 && bad) atomicOr(&C->status, kStNonFinite);
+}
+
+void launch_kick_drift(const Particles& P, long long n, float hdt, float dt, bool split, Counters* C,
+                       cudaStream_t s) {
+    const unsigned b = grid_for(n, 256, 152 * 8);
+    if (split)
+        kick_drift_kernel<true><<<b, 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.acc, hdt, dt, C);
+    else
+        kick_drift_kernel<false><<<b, 256, 0, s>>>(n, P.pos, nullptr, P.vel, P.acc, hdt, dt, C);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 diagnostics
+// ---------------------------------------------------------------------------
+
+constexpr int kDiagThreads = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+    return t;
+}
+
+__device__ __forceinline__ void load_state_d(long long i, const float4* pos, const float4* plo, const float4* vel,
+                                             double& x, double& y, double& z, double& vx, double& vy, double& vz,
+                                             double& m) {
+    const float4 p = pos[i];
+    x = p.x;
+    y = p.y;
+    z = p.z;
+    if (plo) {
+        const float4 l = plo[i];
+        x += (double)l.x;
+        y += (double)l.y;
+        z += (double)l.z;
+    }
+    m = p.w;
+    const float4 v = vel[i];
+    vx = v.x;
+    vy = v.y;
+    vz = v.z;
+}
+
+// Pass 1: per block {M, Mx, My, Mz, KE, Px, Py, Pz}.
+__global__ void __launch_bounds__(kDiagThreads) diag_pass1_kernel(long long n, const float4* __restrict__ pos,
+                                                                  const float4* __restrict__ plo,
+                                                                  const float4* __restrict__ vel,
+                                                                  double* __restrict__ partial) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double x, y, z, vx, vy, vz, m;
+        load_state_d(i, pos, plo, vel, x, y, z, vx, vy, vz, m);
+        acc[0] += m;
+        acc[1] += m * x;
+        acc[2] += m * y;
+        acc[3] += m * z;
+        acc[4] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        acc[5] += m * vx;
+        acc[6] += m * vy;
+        acc[7] += m * vz;
+    }
+    __shared__ double sh[32];
+    for (int k = 0; k < 8; ++k) {
+        const double t = block_sum_d(acc[k], sh);
+        if (threadIdx.x == 0) partial[blockIdx.x * 8 + k] = t;
+    }
+}
+
+// Pass 2: per block {Lx, Ly, Lz} about the given COM.
+__global__ void __launch_bounds__(kDiagThreads) diag_pass2_kernel(long long n, const float4* __restrict__ pos,
+                                                                  const float4* __restrict__ plo,
+                                                                  const float4* __restrict__ vel, double cx,
+                                                                  double cy, double cz, double* __restrict__ partial) {
+    double L[3] = {0, 0, 0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double x, y, z, vx, vy, vz, m;
+        load_state_d(i, pos, plo, vel, x, y, z, vx, vy, vz, m);
+        const double rx = x - cx, ry = y - cy, rz = z - cz;
+        L[0] += m * (ry * vz - vy * rz);
+        L[1] += m * (rz * vx - vz * rx);
+        L[2] += m * (rx * vy - vx * ry);
+    }
+    __shared__ double sh[32];
+    for (int k = 0; k < 3; ++k) {
+        const double t = block_sum_d(L[k], sh);
+        if (threadIdx.x == 0) partial[blockIdx.x * 3 + k] = t;
+    }
+}
+
+int diag_blocks(long long n) { return (int)grid_for(n, kDiagThreads, 152 * 2); }
+
+void launch_diag_pass1(long long n, const Particles& P, bool split, double* partial, cudaStream_t s) {
+    diag_pass1_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel, partial);
+}
+
+void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, double cy, double cz, double* partial,
+                       cudaStream_t s) {
+    diag_pass2_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel, cx, cy, cz,
+                                                              partial);
+}
+
+// Exact pair potential: thread i sums j > i over shared-memory tiles, in FP64.
+constexpr int kPotThreads = 256;
+
+__global__ void __launch_bounds__(kPotThreads) potential_kernel(long long n, const float4* __restrict__ pos,
+                                                                const float4* __restrict__ plo, double eps2,
+                                                                double* __restrict__ partial) {
+    __shared__ double sx[kPotThreads], sy[kPotThreads], sz[kPotThreads], sm[kPotThreads];
+    __shared__ double red[32];
+    const long long i = blockIdx.x * (long long)kPotThreads + threadIdx.x;
+    double xi = 0, yi = 0, zi = 0, mi = 0;
+    if (i < n) {
+        const float4 p = pos[i];
+        xi = p.x;
+        yi = p.y;
+        zi = p.z;
+        mi = p.w;
+        if (plo) {
+            const float4 l = plo[i];
+            xi += (double)l.x;
+            yi += (double)l.y;
+            zi += (double)l.z;
+        }
+    }
+    double local = 0.0;
+    const long long first_tile = blockIdx.x * (long long)kPotThreads;
+    for (long long t = first_tile; t < n; t += kPotThreads) {
+        const long long j = t + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            const float4 p = pos[j];
+            double x = p.x, y = p.y, z = p.z;
+            if (plo) {
+                const float4 l = plo[j];
+                x += (double)l.x;
+                y += (double)l.y;
+                z += (double)l.z;
+            }
+            sx[threadIdx.x] = x;
+            sy[threadIdx.x] = y;
+            sz[threadIdx.x] = z;
+            sm[threadIdx.x] = p.w;
+        }
+        __syncthreads();
+        if (i < n) {
+            const int kmax = (int)min((long long)kPotThreads, n - t);
+            for (int k = 0; k < kmax; ++k) {
+                if (t + k <= i) continue;
+                const double dx = sx[k] - xi, dy = sy[k] - yi, dz = sz[k] - zi;
+                const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                local -= sm[k] * rsqrt(r2);
+            }
+        }
+    }
+    local *= mi;
+    const double t = block_sum_d(local, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+int potential_blocks(long long n) { return (int)((n + kPotThreads - 1) / kPotThreads); }
+
+void launch_potential(long long n, const Particles& P, bool split, double eps2, double* partial, cudaStream_t s) {
+    potential_kernel<<<potential_blocks(n), kPotThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, eps2, partial);
+}
+
+// ---------------------------------------------------------------------------
+// Direct-sum force-error sampler: one block per target slot.
+// ---------------------------------------------------------------------------
+
+constexpr int kSampThreads = 256;
+
+template <bool FP64PAIRS>
+__global__ void __launch_bounds__(kSampThreads) sampler_kernel(long long n, const float4* __restrict__ pos,
+                                                               const float4* __restrict__ plo,
+                                                               const int* __restrict__ slots, double eps2,
+                                                               double* __restrict__ out) {
+    __shared__ double red[32];
+    const int ti = slots[blockIdx.x];
+    const float4 tp = pos[ti];
+    const float4 tl = plo ? plo[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (FP64PAIRS) {
+        const double xi = (double)tp.x + (double)tl.x, yi = (double)tp.y + (double)tl.y,
+                     zi = (double)tp.z + (double)tl.z;
+        for (long long j = threadIdx.x; j < n; j += kSampThreads) {
+            if (j == ti) continue;
+            const float4 p = pos[j];
+            double x = p.x, y = p.y, z = p.z;
+            if (plo) {
+                const float4 l = plo[j];
+                x += (double)l.x;
+                y += (double)l.y;
+                z += (double)l.z;
+            }
+            const double dx = x - xi, dy = y - yi, dz = z - zi;
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double inv = rsqrt(r2);
+            const double s = (double)p.w * inv * inv * inv;
+            ax += s * dx;
+            ay += s * dy;
+            az += s * dz;
+        }
+    } else {
+        const float e2 = (float)eps2;
+        long long j = threadIdx.x;
+        while (j < n) {
+            float px = 0.f, py = 0.f, pz = 0.f;
+            for (int c = 0; c < 64 && j < n; ++c, j += kSampThreads) {
+                if (j == ti) continue;
+                const float4 p = pos[j];
+                float dx = p.x - tp.x, dy = p.y - tp.y, dz = p.z - tp.z;
+                if (plo) {
+                    const float4 l = plo[j];
+                    dx += l.x - tl.x;
+                    dy += l.y - tl.y;
+                    dz += l.z - tl.z;
+                }
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
+                const float inv = rsqrtf(r2);
+                const float f = p.w * inv * inv * inv;
+                px = fmaf(f, dx, px);
+                py = fmaf(f, dy, py);
+                pz = fmaf(f, dz, pz);
+            }
+            ax += px;
+            ay += py;
+            az += pz;
+        }
+    }
+    const double sx = block_sum_d(ax, red);
+    const double sy = block_sum_d(ay, red);
+    const double sz = block_sum_d(az, red);
+    if (threadIdx.x == 0) {
+        out[3 * blockIdx.x + 0] = sx;
+        out[3 * blockIdx.x + 1] = sy;
+        out[3 * blockIdx.x + 2] = sz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 FMA throughput probe: 8 independent register-resident FMA chains per
+// thread, no memory traffic inside the loop.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) fma_probe_kernel(float* __restrict__ out, int iters, float a, float b) {
+    float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f, x4 = x0 + 4.f, x5 = x0 + 5.f,
+          x6 = x0 + 6.f, x7 = x0 + 7.f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            x0 = fmaf(x0, a, b);
+            x1 = fmaf(x1, a, b);
+            x2 = fmaf(x2, a, b);
+            x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b);
+            x5 = fmaf(x5, a, b);
+            x6 = fmaf(x6, a, b);
+            x7 = fmaf(x7, a, b);
+        }
+    }
+    const float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 12345.678f) out[blockIdx.x] = s;  // keeps the chains live
+}
+
+// Returns TFLOP/s (2 flops per FMA) of one timed launch after a warm-up.
+double run_fma_probe(int sm_count, cudaStream_t s) {
+    const int blocks = sm_count * 8, threads = 256, iters = 1024;
+    float* out = nullptr;
+    if (cudaMalloc(&out, sizeof(float) * blocks) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fma_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.9999999f, 1e-7f);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0, s);
+        fma_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.9999999f, 1e-7f);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double fmas = (double)blocks * threads * iters * 64.0;
+    return 2.0 * fmas / (best * 1e-3) / 1e12;
+}
+
+void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
+                    bool fp64_pairs, double* out, cudaStream_t s) {
+    if (nslots <= 0) return;
+    if (fp64_pairs)
+        sampler_kernel<true><<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
+    else
+        sampler_kernel<false><<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
+}
+
+}  // namespace ngrav

@@ -1,0 +1,456 @@
+// keys_sort.cu -- bounding box, 63-bit octant-path keys, stable LSD radix
+// sort of (key, slot) pairs, device-wide exclusive scan and the gather that
+// puts the particle state into key order.
+//
+// Bit-exactness with the reference tree (projects/nbody_core/src/Tree.cpp):
+//  * the root cube is the FP64 bounding box of the positions, centre
+//    0.5*(lo+hi), half = max half extent (1.0 if <= 1e-12) times 1.001
+//    (Tree.cpp:54-88);
+//  * at each level the octant bit per axis is (p >= centre) (Tree.cpp:11-20)
+//    and the child centre is centre +/- 0.5*half, rounded in FP64 exactly as
+//    NewChild does (Tree.cpp:90-112).
+// Key digit l (bits 3*(20-l)..+2) is the octant (x:1, y:2, z:4) of the
+// particle's level-l ancestor, so ascending keys enumerate leaves in the
+// reference's DFS ascending-octant order (Tree.cpp:157-175).
+#include "engine.cuh"
+
+#include <cstdio>
+
+namespace ngrav {
+
+// ---------------------------------------------------------------------------
+// FP64 bounding box with order-preserving integer atomics
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long enc_f64(double d) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ double dec_f64(unsigned long long u) {
+    u = (u & 0x8000000000000000ull) ? (u & 0x7FFFFFFFFFFFFFFFull) : ~u;
+    return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ double pos_d(const float4& hi, const float4* plo, long long i, int axis) {
+    const float h = axis == 0 ? hi.x : (axis == 1 ? hi.y : hi.z);
+    if (!plo) return (double)h;
+    const float4 lo = plo[i];
+    const float l = axis == 0 ? lo.x : (axis == 1 ? lo.y : lo.z);
+    return (double)h + (double)l;
+}
+
+constexpr int kBoxThreads = 256;
+
+__global__ void __launch_bounds__(kBoxThreads) bbox_kernel(const float4* __restrict__ pos,
+                                                           const float4* __restrict__ plo, long long n,
+                                                           Counters* C) {
+    double lo[3] = {1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0};
+    double hi[3] = {-1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0};
+    bool bad = false;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        bad |= !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(p.w));
+        for (int a = 0; a < 3; ++a) {
+            const double v = pos_d(p, plo, i, a);
+            lo[a] = fmin(lo[a], v);
+            hi[a] = fmax(hi[a], v);
+        }
+    }
+    __shared__ double slo[3][kBoxThreads / 32], shi[3][kBoxThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int a = 0; a < 3; ++a) {
+        double l = lo[a], h = hi[a];
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+            h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+        }
+        if (lane == 0) {
+            slo[a][w] = l;
+            shi[a][w] = h;
+        }
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        double l = slo[a][0], h = shi[a][0];
+        for (int k = 1; k < kBoxThreads / 32; ++k) {
+            l = fmin(l, slo[a][k]);
+            h = fmax(h, shi[a][k]);
+        }
+        atomicMin(&C->bbox_min[a], enc_f64(l));
+        atomicMax(&C->bbox_max[a], enc_f64(h));
+    }
+    if (threadIdx.x == 0 && bad) atomicOr(&C->status, kStNonFinite);
+}
+
+// Root cube of BuildRoot (Tree.cpp:54-88), once per evaluation.
+__global__ void root_kernel(Counters* C, long long n) {
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = n > 0 ? dec_f64(C->bbox_min[a]) : 0.0;
+        hi[a] = n > 0 ? dec_f64(C->bbox_max[a]) : 0.0;
+    }
+    double half = __dmul_rn(0.5, __dsub_rn(hi[0], lo[0]));
+    const double hy = __dmul_rn(0.5, __dsub_rn(hi[1], lo[1]));
+    const double hz = __dmul_rn(0.5, __dsub_rn(hi[2], lo[2]));
+    if (half < hy) half = hy;
+    if (half < hz) half = hz;
+    if (!(half > 1e-12)) half = 1.0;
+    for (int a = 0; a < 3; ++a) C->root_center[a] = __dmul_rn(0.5, __dadd_rn(lo[a], hi[a]));
+    C->root_half = __dmul_rn(half, 1.001);
+}
+
+void launch_bbox(const float4* pos, const float4* plo, long long n, Counters* C, cudaStream_t s) {
+    long long blocks = (n + kBoxThreads - 1) / kBoxThreads;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    bbox_kernel<<<(unsigned)blocks, kBoxThreads, 0, s>>>(pos, plo, n, C);
+}
+
+void launch_root(Counters* C, long long n, cudaStream_t s) { root_kernel<<<1, 1, 0, s>>>(C, n); }
+
+// SPLIT -> PLAIN: fold the low halves into FP32 positions.
+__global__ void collapse_split_kernel(float4* __restrict__ pos, float4* __restrict__ plo, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 p = pos[i];
+        const float4 l = plo[i];
+        p.x = (float)((double)p.x + (double)l.x);
+        p.y = (float)((double)p.y + (double)l.y);
+        p.z = (float)((double)p.z + (double)l.z);
+        pos[i] = p;
+        plo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    collapse_split_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, plo, n);
+}
+
+// ---------------------------------------------------------------------------
+// 63-bit keys by the reference's FP64 centre recurrence
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned axis_bits(double p, double c, double h) {
+    // Returns 21 octant bits of one axis, level 0 in bit 20.
+    unsigned bits = 0;
+#pragma unroll
+    for (int l = 0; l < kKeyLevels; ++l) {
+        const bool b = p >= c;
+        bits = (bits << 1) | (b ? 1u : 0u);
+        h = __dmul_rn(0.5, h);
+        c = b ? __dadd_rn(c, h) : __dsub_rn(c, h);
+    }
+    return bits;
+}
+
+// Spread 21 bits so bit k lands at 3k.
+__device__ __forceinline__ unsigned long long spread3(unsigned v) {
+    unsigned long long x = v & 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ pos, const float4* __restrict__ plo,
+                                                   long long n, const Counters* __restrict__ C,
+                                                   unsigned long long* __restrict__ keys,
+                                                   unsigned* __restrict__ vals) {
+    const double cx = C->root_center[0], cy = C->root_center[1], cz = C->root_center[2];
+    const double h0 = C->root_half;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        double px = p.x, py = p.y, pz = p.z;
+        if (plo) {
+            const float4 l = plo[i];
+            px += (double)l.x;
+            py += (double)l.y;
+            pz += (double)l.z;
+        }
+        const unsigned bx = axis_bits(px, cx, h0);
+        const unsigned by = axis_bits(py, cy, h0);
+        const unsigned bz = axis_bits(pz, cz, h0);
+        keys[i] = spread3(bx) | (spread3(by) << 1) | (spread3(bz) << 2);
+        vals[i] = (unsigned)i;
+    }
+}
+
+void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, unsigned long long* keys,
+                 unsigned* vals, cudaStream_t s) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    keys_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, plo, n, C, keys, vals);
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide exclusive scan of unsigned (reduce / scan partials / downsweep)
+// ---------------------------------------------------------------------------
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+long long scan_tmp_size(long long n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* s_warp, unsigned& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        unsigned t = lane < nw ? s_warp[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) s_warp[lane] = t;
+    }
+    __syncthreads();
+    total = s_warp[nw - 1];
+    const unsigned before = w > 0 ? s_warp[w - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const unsigned* __restrict__ in, long long n,
+                                                                   unsigned* __restrict__ partial) {
+    const long long base = blockIdx.x * (long long)kScanTile;
+    unsigned s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long i = base + k * kScanThreads + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ unsigned ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int k = 0; k < kScanThreads / 32; ++k) t += ws[k];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) scan_partials_kernel(unsigned* partial, int nb) {
+    __shared__ unsigned s_warp[32];
+    unsigned carry = 0;
+    for (int base = 0; base < nb; base += 1024) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < nb ? partial[i] : 0u;
+        unsigned total;
+        const unsigned ex = block_exclusive_scan(v, s_warp, total);
+        if (i < nb) partial[i] = carry + ex;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const unsigned* __restrict__ in, long long n,
+                                                                 const unsigned* __restrict__ partial,
+                                                                 unsigned* __restrict__ out) {
+    __shared__ unsigned s_warp[32];
+    const long long base = blockIdx.x * (long long)kScanTile + (long long)threadIdx.x * kScanItems;
+    unsigned v[kScanItems];
+    unsigned sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long i = base + k;
+        v[k] = i < n ? in[i] : 0u;
+        sum += v[k];
+    }
+    unsigned total;
+    unsigned run = block_exclusive_scan(sum, s_warp, total) + partial[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const long long i = base + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+}
+
+void device_exclusive_scan(const unsigned* in, unsigned* out, long long n, unsigned* tmp, cudaStream_t s) {
+    if (n <= 0) return;
+    const int nb = (int)((n + kScanTile - 1) / kScanTile);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, s>>>(in, n, tmp);
+    scan_partials_kernel<<<1, 1024, 0, s>>>(tmp, nb);
+    scan_down_kernel<<<nb, kScanThreads, 0, s>>>(in, n, tmp, out);
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits, 4096-key tiles
+// ---------------------------------------------------------------------------
+
+constexpr int kRsThreads = 256;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsItems = 16;
+constexpr int kRsTile = kRsThreads * kRsItems;   // 4096
+constexpr int kRsWarpSpan = 32 * kRsItems;       // 512 consecutive keys per warp
+
+// Histogram of one digit per tile, digit-major: hist[d * nblocks + b].
+__global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const unsigned long long* __restrict__ keys,
+                                                             long long n, int shift, unsigned* __restrict__ hist) {
+    __shared__ unsigned h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long base = blockIdx.x * (long long)kRsTile + w * kRsWarpSpan + lane;
+#pragma unroll 4
+    for (int k = 0; k < kRsItems; ++k) {
+        const long long i = base + k * 32;
+        const unsigned d = i < n ? (unsigned)(keys[i] >> shift) & 255u : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < 256u && (__ffs(peers) - 1) == lane) atomicAdd(&h[d], (unsigned)__popc(peers));
+    }
+    __syncthreads();
+    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned long long* __restrict__ kin,
+                                                                const unsigned* __restrict__ vin,
+                                                                unsigned long long* __restrict__ kout,
+                                                                unsigned* __restrict__ vout, long long n, int shift,
+                                                                const unsigned* __restrict__ hist_scan) {
+    extern __shared__ unsigned long long rs_smem[];
+    unsigned long long* skeys = rs_smem;                          // kRsTile
+    unsigned* svals = reinterpret_cast<unsigned*>(skeys + kRsTile);  // kRsTile
+    __shared__ unsigned warp_cnt[kRsWarps][256];
+    __shared__ unsigned digit_start[256];   // block-local exclusive prefix over digits
+    __shared__ unsigned digit_base[256];    // global output offset of (digit, block)
+    __shared__ unsigned s_warp[32];
+
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k < kRsWarps * 256; k += kRsThreads) (&warp_cnt[0][0])[k] = 0;
+    __syncthreads();
+
+    const long long tile = blockIdx.x * (long long)kRsTile;
+    const long long base = tile + w * kRsWarpSpan + lane;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    unsigned long long key[kRsItems];
+    unsigned val[kRsItems];
+    unsigned short rank[kRsItems];
+#pragma unroll
+    for (int k = 0; k < kRsItems; ++k) {
+        const long long i = base + k * 32;
+        const bool valid = i < n;
+        key[k] = valid ? kin[i] : 0ull;
+        val[k] = valid ? vin[i] : 0u;
+        const unsigned d = valid ? (unsigned)(key[k] >> shift) & 255u : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        unsigned before = 0;
+        if (valid) before = warp_cnt[w][d];
+        __syncwarp();
+        if (valid) {
+            rank[k] = (unsigned short)(before + __popc(peers & lt_mask));
+            if ((__ffs(peers) - 1) == lane) warp_cnt[w][d] = before + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    // Per digit: exclusive prefix over warps (stable: warp w precedes w+1).
+    const unsigned d = threadIdx.x;
+    unsigned run = 0;
+#pragma unroll
+    for (int ww = 0; ww < kRsWarps; ++ww) {
+        const unsigned c = warp_cnt[ww][d];
+        warp_cnt[ww][d] = run;
+        run += c;
+    }
+    unsigned total;
+    const unsigned ds = block_exclusive_scan(run, s_warp, total);
+    digit_start[d] = ds;
+    digit_base[d] = hist_scan[d * gridDim.x + blockIdx.x];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRsItems; ++k) {
+        const long long i = base + k * 32;
+        if (i < n) {
+            const unsigned dd = (unsigned)(key[k] >> shift) & 255u;
+            const unsigned r = digit_start[dd] + warp_cnt[w][dd] + rank[k];
+            skeys[r] = key[k];
+            svals[r] = val[k];
+        }
+    }
+    __syncthreads();
+    long long nvalid = n - tile;
+    if (nvalid > kRsTile) nvalid = kRsTile;
+    for (int j = threadIdx.x; j < nvalid; j += kRsThreads) {
+        const unsigned long long kk = skeys[j];
+        const unsigned dd = (unsigned)(kk >> shift) & 255u;
+        const unsigned o = digit_base[dd] + (unsigned)j - digit_start[dd];
+        kout[o] = kk;
+        vout[o] = svals[j];
+    }
+}
+
+void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s) {
+    if (n <= 1) return;
+    const int nb = (int)((n + kRsTile - 1) / kRsTile);
+    const size_t smem = (size_t)kRsTile * (sizeof(unsigned long long) + sizeof(unsigned));
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaFuncSetAttribute(rs_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_done = true;
+    }
+    unsigned long long* kin = sb.keys;
+    unsigned long long* kout = sb.keys_alt;
+    unsigned* vin = sb.vals;
+    unsigned* vout = sb.vals_alt;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        rs_hist_kernel<<<nb, kRsThreads, 0, s>>>(kin, n, shift, sb.hist);
+        device_exclusive_scan(sb.hist, sb.hist, (long long)nb * 256, sb.scan_tmp, s);
+        rs_scatter_kernel<<<nb, kRsThreads, smem, s>>>(kin, vin, kout, vout, n, shift, sb.hist);
+        unsigned long long* tk = kin;
+        kin = kout;
+        kout = tk;
+        unsigned* tv = vin;
+        vin = vout;
+        vout = tv;
+    }
+    if (passes & 1) {
+        cudaMemcpyAsync(sb.keys, kin, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(sb.vals, vin, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gather the state into key order: new[k] = old[perm[k]] (into the *2 buffers)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) permute_kernel(const unsigned* __restrict__ perm, long long n,
+                                                      const float4* __restrict__ pos, const float4* __restrict__ plo,
+                                                      const float4* __restrict__ vel, const float4* __restrict__ acc,
+                                                      const int* __restrict__ id, float4* __restrict__ pos2,
+                                                      float4* __restrict__ plo2, float4* __restrict__ vel2,
+                                                      float4* __restrict__ acc2, int* __restrict__ id2) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const unsigned j = perm[k];
+        pos2[k] = pos[j];
+        if (plo) plo2[k] = plo[j];
+        vel2[k] = vel[j];
+        acc2[k] = acc[j];
+        id2[k] = id[j];
+    }
+}
+
+void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s) {
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    permute_kernel<<<(unsigned)blocks, 256, 0, s>>>(perm, n, P.pos, split ? P.plo : nullptr, P.vel, P.acc, P.id,
+                                                     P.pos2, split ? P.plo2 : nullptr, P.vel2, P.acc2, P.id2);
+}
+
+}  // namespace ngrav

@@ -1,0 +1,344 @@
+// tree.cu -- linear octree from sorted keys, leaf list, upward moment pass.
+//
+// Topology rule (restating projects/nbody_core/src/Tree.cpp:114-145): a node
+// at level l whose particle count exceeds the leaf capacity (ncrit) and whose
+// level is below maxDepth is internal; its children are its non-empty
+// octants.  The node set of the reference's insertion build is exactly this
+// set, independent of insertion order, so it is built here top-down, one
+// level per launch, by splitting each internal node's contiguous key range at
+// its level-l digit boundaries (binary search).  Children of a node are
+// allocated contiguously in ascending octant order.
+//
+// Moments (restating Tree.cpp:119-122 running COM, :179-202 maxRadius,
+// :205-254 quadrupoles): leaves sum their members (mass and COM in FP64,
+// quadrupole in FP32 on offsets from the COM); internal nodes combine their
+// children in FP64 (the top-level moment accumulation), bottom-up with
+// per-node arrival counters so each parent is finished by the last child to
+// arrive.
+#include "engine.cuh"
+
+namespace ngrav {
+
+__global__ void reset_counters_kernel(Counters* C) {
+    if (threadIdx.x == 0) {
+        Counters z{};
+        for (int a = 0; a < 3; ++a) {
+            z.bbox_min[a] = ~0ull;
+            z.bbox_max[a] = 0ull;
+        }
+        *C = z;
+    }
+}
+
+__global__ void tree_init_kernel(NodeArrays T, Counters* C, long long n, int leaf_cap, int max_depth) {
+    T.start[0] = 0;
+    T.count[0] = (int)n;
+    T.first_child[0] = -1;
+    T.parent[0] = -1;
+    T.visit[0] = 0;
+    T.nchild[0] = 0;
+    T.level[0] = 0;
+    T.cx[0] = C->root_center[0];
+    T.cy[0] = C->root_center[1];
+    T.cz[0] = C->root_center[2];
+    C->next_free = 1;
+    C->level_begin[0] = 0;
+    C->level_begin[1] = 1;
+    C->levels_used = 0;
+    C->max_leaf_count = 0;
+}
+
+void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s) {
+    tree_init_kernel<<<1, 1, 0, s>>>(T, C, n, leaf_cap, max_depth);
+}
+
+// First index k in [lo, hi) whose level digit (at `shift`) is >= d.
+__device__ __forceinline__ int digit_lower_bound(const unsigned long long* __restrict__ keys, int lo, int hi,
+                                                 int shift, unsigned d) {
+    while (lo < hi) {
+        const int mid = lo + ((hi - lo) >> 1);
+        const unsigned v = (unsigned)(__ldg(keys + mid) >> shift) & 7u;
+        if (v < d)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+constexpr int kLevelThreads = 256;
+
+__global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T, Counters* C,
+                                                                   const unsigned long long* __restrict__ keys,
+                                                                   int l, int leaf_cap, int max_depth) {
+    const int begin = C->level_begin[l];
+    const int end = C->level_begin[l + 1];
+    const int shift = 3 * (kKeyLevels - 1 - l);
+    const double child_half = ldexp(C->root_half, -(l + 1));
+    for (int node = begin + blockIdx.x * blockDim.x + threadIdx.x; node < end; node += gridDim.x * blockDim.x) {
+        const int cnt = T.count[node];
+        if (!(cnt > leaf_cap && l < max_depth)) continue;  // stays a leaf
+        const int s = T.start[node];
+        const int e = s + cnt;
+        int bnd[9];
+        bnd[0] = s;
+        bnd[8] = e;
+        int lo = s;
+#pragma unroll
+        for (unsigned d = 1; d < 8; ++d) {
+            lo = digit_lower_bound(keys, lo, e, shift, d);
+            bnd[d] = lo;
+        }
+        int nch = 0;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) nch += bnd[d + 1] > bnd[d];
+        const int base = atomicAdd(&C->next_free, nch);
+        if (base + nch > T.cap) {
+            atomicOr(&C->status, kStNodeOverflow);
+            continue;
+        }
+        const double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
+        int c = base;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            const int cs = bnd[d], ce = bnd[d + 1];
+            if (ce <= cs) continue;
+            T.start[c] = cs;
+            T.count[c] = ce - cs;
+            T.first_child[c] = -1;
+            T.parent[c] = node;
+            T.visit[c] = 0;
+            T.nchild[c] = 0;
+            T.level[c] = (unsigned char)(l + 1);
+            T.cx[c] = (d & 1) ? __dadd_rn(pcx, child_half) : __dsub_rn(pcx, child_half);
+            T.cy[c] = (d & 2) ? __dadd_rn(pcy, child_half) : __dsub_rn(pcy, child_half);
+            T.cz[c] = (d & 4) ? __dadd_rn(pcz, child_half) : __dsub_rn(pcz, child_half);
+            if (l + 1 >= kKeyLevels && ce - cs > leaf_cap && l + 1 < max_depth) {
+                atomicOr(&C->status, kStDepthLimit);
+                atomicAdd(&C->depth_limited, 1);
+            }
+            ++c;
+        }
+        T.first_child[node] = base;
+        T.nchild[node] = (unsigned char)nch;
+        atomicMax(&C->levels_used, l + 1);
+    }
+    // The last block to finish publishes where level l+2 begins.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int prev = atomicAdd(&C->done_blocks, 1);
+        if (prev == (int)gridDim.x - 1) {
+            int nf = atomicAdd(&C->next_free, 0);
+            if (nf > T.cap) nf = T.cap;
+            C->level_begin[l + 2] = nf;
+            C->done_blocks = 0;
+        }
+    }
+}
+
+void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
+                        int max_depth, cudaStream_t s) {
+    // Enough threads for the widest level (nodes <= cap); levels above it
+    // exit after a bounds check.
+    long long blocks = ((long long)T.cap / 4 + kLevelThreads - 1) / kLevelThreads;
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    if (blocks < 1) blocks = 1;
+    for (int l = 0; l < kKeyLevels; ++l)
+        tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth);
+}
+
+// ---------------------------------------------------------------------------
+// Leaf list in key order
+// ---------------------------------------------------------------------------
+
+__global__ void leaf_mark_kernel(NodeArrays T, Counters* C, int* __restrict__ leaf_at,
+                                 unsigned* __restrict__ flags) {
+    const int nn = min(C->next_free, T.cap);
+    for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < nn; node += gridDim.x * blockDim.x) {
+        if (T.first_child[node] != -1) continue;
+        const int s = T.start[node];
+        leaf_at[s] = node;
+        flags[s] = 1u;
+        atomicMax(&C->max_leaf_count, T.count[node]);
+    }
+}
+
+__global__ void leaf_compact_kernel(const int* __restrict__ leaf_at, const unsigned* __restrict__ flags,
+                                    const unsigned* __restrict__ pos, long long n, int* __restrict__ leaf_list,
+                                    Counters* C) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        if (flags[k]) leaf_list[pos[k]] = leaf_at[k];
+        if (k == n - 1) C->nleaves = (int)(pos[k] + flags[k]);
+    }
+}
+
+void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, unsigned* flags, unsigned* scan_out,
+                      int* leaf_list, SortBuffers& sb, cudaStream_t s) {
+    cudaMemsetAsync(flags, 0, sizeof(unsigned) * n, s);
+    long long b1 = ((long long)T.cap + 255) / 256;
+    if (b1 > 152 * 8) b1 = 152 * 8;
+    leaf_mark_kernel<<<(unsigned)b1, 256, 0, s>>>(T, C, leaf_at, flags);
+    device_exclusive_scan(flags, scan_out, n, sb.scan_tmp, s);
+    long long b2 = (n + 255) / 256;
+    if (b2 > 152 * 8) b2 = 152 * 8;
+    leaf_compact_kernel<<<(unsigned)b2, 256, 0, s>>>(leaf_at, flags, scan_out, n, leaf_list, C);
+}
+
+// ---------------------------------------------------------------------------
+// Upward pass
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float round_up_f(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = nextafterf(f, 3.0e38f);
+    return f;
+}
+
+__device__ __forceinline__ void write_walk_record(NodeArrays& T, int node, double M, double cx, double cy,
+                                                  double cz, const double* Q, double maxr, bool leaf, int link,
+                                                  int cnt_or_nch, int level, double root_half) {
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    T.wA[node] = make_float4(hx, hy, hz, (float)M);
+    T.wB[node] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
+    const double size = 2.0 * ldexp(root_half, -level);
+    T.wC[node] = make_float4((float)Q[4], (float)size, __int_as_float(link),
+                             __int_as_float(meta_pack(leaf, cnt_or_nch, level)));
+    T.wD[node] = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy), (float)(cz - (double)hz),
+                             round_up_f(maxr));
+}
+
+__global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C, const float4* __restrict__ pos,
+                                                      const float4* __restrict__ plo, float4* __restrict__ src,
+                                                      const int* __restrict__ leaf_list, int split, int quadrupole) {
+    const int nleaves = C->nleaves;
+    const double root_half = C->root_half;
+    for (int li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
+        const int leaf = leaf_list[li];
+        const int s = T.start[leaf], cnt = T.count[leaf];
+        double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+        for (int j = s; j < s + cnt; ++j) {
+            const float4 p = pos[j];
+            double x = p.x, y = p.y, z = p.z;
+            if (plo) {
+                const float4 q = plo[j];
+                x += (double)q.x;
+                y += (double)q.y;
+                z += (double)q.z;
+            }
+            const double m = p.w;
+            M += m;
+            Sx = fma(m, x, Sx);
+            Sy = fma(m, y, Sy);
+            Sz = fma(m, z, Sz);
+        }
+        const double ccx = T.cx[leaf], ccy = T.cy[leaf], ccz = T.cz[leaf];
+        double cx = ccx, cy = ccy, cz = ccz;
+        if (M > 0.0) {
+            cx = Sx / M;
+            cy = Sy / M;
+            cz = Sz / M;
+        }
+        double maxr2 = 0.0;
+        float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f, q4 = 0.f;
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = s; j < s + cnt; ++j) {
+            const float4 p = pos[j];
+            const float4 l = plo ? plo[j] : zero4;
+            const double x = (double)p.x + (double)l.x, y = (double)p.y + (double)l.y, z = (double)p.z + (double)l.z;
+            const double dx = x - cx, dy = y - cy, dz = z - cz;
+            maxr2 = fmax(maxr2, dx * dx + dy * dy + dz * dz);
+            if (quadrupole && cnt > 1) {
+                const float fx = (float)dx, fy = (float)dy, fz = (float)dz, m = p.w;
+                const float d2 = fx * fx + fy * fy + fz * fz;
+                q0 += m * (3.f * fx * fx - d2);
+                q1 += m * (3.f * fy * fy - d2);
+                q2 += m * 3.f * fx * fy;
+                q3 += m * 3.f * fx * fz;
+                q4 += m * 3.f * fy * fz;
+            }
+            if (split)
+                src[j] = make_float4((float)(x - ccx), (float)(y - ccy), (float)(z - ccz), p.w);
+            else
+                src[j] = p;
+        }
+        const double maxr = sqrt(maxr2);
+        const double Q[5] = {q0, q1, q2, q3, q4};
+        T.mass[leaf] = M;
+        T.comx[leaf] = cx;
+        T.comy[leaf] = cy;
+        T.comz[leaf] = cz;
+        T.maxr[leaf] = maxr;
+        for (int k = 0; k < 5; ++k) T.quad[5 * leaf + k] = Q[k];
+        const int level = T.level[leaf];
+        write_walk_record(T, leaf, M, cx, cy, cz, Q, maxr, true, s, cnt, level, root_half);
+        const float hx = (float)ccx, hy = (float)ccy, hz = (float)ccz;
+        T.chi[leaf] = make_float4(hx, hy, hz, 0.f);
+        T.clo[leaf] = make_float4((float)(ccx - (double)hx), (float)(ccy - (double)hy), (float)(ccz - (double)hz), 0.f);
+
+        // Climb while this thread is the last child to arrive.
+        int node = leaf;
+        for (;;) {
+            const int parent = T.parent[node];
+            if (parent < 0) break;
+            __threadfence();
+            const int nch = T.nchild[parent];
+            const int old = atomicAdd(&T.visit[parent], 1);
+            if (old != nch - 1) break;
+            __threadfence();
+            const int fc = T.first_child[parent];
+            double PM = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+            for (int c = fc; c < fc + nch; ++c) {
+                const double mc = __ldcg(T.mass + c);
+                PM += mc;
+                px = fma(mc, __ldcg(T.comx + c), px);
+                py = fma(mc, __ldcg(T.comy + c), py);
+                pz = fma(mc, __ldcg(T.comz + c), pz);
+            }
+            double pcx = T.cx[parent], pcy = T.cy[parent], pcz = T.cz[parent];
+            if (PM > 0.0) {
+                pcx = px / PM;
+                pcy = py / PM;
+                pcz = pz / PM;
+            }
+            double PQ[5] = {0, 0, 0, 0, 0};
+            double pr = 0.0;
+            for (int c = fc; c < fc + nch; ++c) {
+                const double mc = __ldcg(T.mass + c);
+                const double dx = __ldcg(T.comx + c) - pcx, dy = __ldcg(T.comy + c) - pcy,
+                             dz = __ldcg(T.comz + c) - pcz;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                pr = fmax(pr, __ldcg(T.maxr + c) + sqrt(d2));
+                if (mc <= 0.0) continue;
+                if (quadrupole) {
+                    PQ[0] += __ldcg(T.quad + 5 * c + 0) + mc * (3.0 * dx * dx - d2);
+                    PQ[1] += __ldcg(T.quad + 5 * c + 1) + mc * (3.0 * dy * dy - d2);
+                    PQ[2] += __ldcg(T.quad + 5 * c + 2) + mc * 3.0 * dx * dy;
+                    PQ[3] += __ldcg(T.quad + 5 * c + 3) + mc * 3.0 * dx * dz;
+                    PQ[4] += __ldcg(T.quad + 5 * c + 4) + mc * 3.0 * dy * dz;
+                }
+            }
+            T.mass[parent] = PM;
+            T.comx[parent] = pcx;
+            T.comy[parent] = pcy;
+            T.comz[parent] = pcz;
+            T.maxr[parent] = pr;
+            for (int k = 0; k < 5; ++k) T.quad[5 * parent + k] = PQ[k];
+            write_walk_record(T, parent, PM, pcx, pcy, pcz, PQ, pr, false, fc, nch, T.level[parent], root_half);
+            node = parent;
+        }
+    }
+}
+
+void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,
+                    int max_leaves, bool split, bool quadrupole, cudaStream_t s) {
+    long long blocks = ((long long)max_leaves + 127) / 128;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    moments_kernel<<<(unsigned)blocks, 128, 0, s>>>(T, C, P.pos, split ? P.plo : nullptr, P.src, leaf_list,
+                                                    split ? 1 : 0, quadrupole ? 1 : 0);
+}
+
+void launch_reset_counters(Counters* C, cudaStream_t s) { reset_counters_kernel<<<1, 32, 0, s>>>(C); }
+
+}  // namespace ngrav

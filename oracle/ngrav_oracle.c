@@ -472,6 +472,112 @@ int or_bh_accel(int n, const double* x, const double* y, const double* z, const 
     return 0;
 }
 
+#include <time.h>
+
+static double now_ms(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+int or_bh_time_sampled(int n, const double* x, const double* y, const double* z, const double* m, double G,
+                       double eps, double theta, int ncrit, int quad, int group_stride, double* out) {
+    or_tree t;
+    const double t0 = now_ms();
+    if (or_tree_build(&t, n, x, y, z, m, ncrit, 40)) {
+        or_tree_free(&t);
+        return -1;
+    }
+    if (quad) or_tree_quadrupoles(&t, x, y, z, m);
+    const double t1 = now_ms();
+    /* Walk every group_stride-th leaf group: a leaf subset with a full tree. */
+    const int nn = t.nnodes;
+    int nleaves = 0;
+    for (int i = 0; i < nn; ++i)
+        if (t.nchild[i] == 0 && t.count[i] > 0) ++nleaves;
+    double* ax = (double*)calloc((size_t)n, sizeof(double));
+    double* ay = (double*)calloc((size_t)n, sizeof(double));
+    double* az = (double*)calloc((size_t)n, sizeof(double));
+    long long sampled = 0;
+    int* groups = (int*)malloc(sizeof(int) * (size_t)(nleaves + 1));
+    int ng = 0, li = 0;
+    for (int i = 0; i < nn; ++i) {
+        if (t.nchild[i] == 0 && t.count[i] > 0) {
+            if (li % group_stride == 0) {
+                groups[ng++] = i;
+                sampled += t.count[i];
+            }
+            ++li;
+        }
+    }
+    or_counters cnt;
+    const double t2 = now_ms();
+    {
+        const double theta2 = theta * theta;
+        const double eps2 = eps * eps;
+        int maxlevel = 0;
+        for (int i = 0; i < nn; ++i)
+            if (t.level[i] > maxlevel) maxlevel = t.level[i];
+        long long pairs = 0;
+#pragma omp parallel reduction(+ : pairs)
+        {
+            walk_lists L;
+            memset(&L, 0, sizeof(L));
+            L.capstack = 8 * (maxlevel + 2) + 8;
+            L.stack = (int*)malloc(sizeof(int) * (size_t)L.capstack);
+#pragma omp for schedule(dynamic, 32)
+            for (int gi = 0; gi < ng; ++gi) {
+                const int g = groups[gi];
+                collect(&t, g, theta2, &L);
+                const int lo = t.first[g], hi = lo + t.count[g];
+                for (int k = lo; k < hi; ++k) {
+                    const int i = t.order[k];
+                    const double xi = x[i], yi = y[i], zi = z[i];
+                    double axi = 0.0, ayi = 0.0, azi = 0.0;
+                    for (int f = 0; f < L.nfar; ++f) {
+                        const int nd = L.far[f];
+                        const double dx = t.comx[nd] - xi, dy = t.comy[nd] - yi, dz = t.comz[nd] - zi;
+                        const double dist2 = dx * dx + dy * dy + dz * dz;
+                        accum_pair(dx, dy, dz, G * t.mass[nd], eps2, &axi, &ayi, &azi);
+                        if (t.has_quad) add_quadrupole(t.q + 5 * nd, dx, dy, dz, dist2, G, &axi, &ayi, &azi);
+                    }
+                    for (int l = 0; l < L.nnear; ++l) {
+                        const int lf = L.near[l];
+                        for (int k2 = t.first[lf]; k2 < t.first[lf] + t.count[lf]; ++k2) {
+                            const int p = t.order[k2];
+                            accum_pair(x[p] - xi, y[p] - yi, z[p] - zi, G * m[p], eps2, &axi, &ayi, &azi);
+                        }
+                        pairs += t.count[lf];
+                    }
+                    for (int k2 = lo; k2 < hi; ++k2) {
+                        if (k2 == k) continue;
+                        const int p = t.order[k2];
+                        accum_pair(x[p] - xi, y[p] - yi, z[p] - zi, G * m[p], eps2, &axi, &ayi, &azi);
+                    }
+                    ax[i] = axi;
+                    ay[i] = ayi;
+                    az[i] = azi;
+                }
+            }
+            free(L.far);
+            free(L.near);
+            free(L.stack);
+        }
+        free(groups);
+        cnt.p2p_pairs = pairs;
+    }
+    const double t3 = now_ms();
+    free(ax);
+    free(ay);
+    free(az);
+    or_tree_free(&t);
+    out[0] = t1 - t0;                              /* tree build + quadrupoles, full */
+    out[1] = t3 - t2;                              /* walk over the sampled groups */
+    out[2] = (double)sampled / (n > 0 ? n : 1);    /* fraction of targets walked */
+    out[3] = (double)cnt.p2p_pairs;
+    return 0;
+}
+
 void or_direct(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps2,
                double* ax, double* ay, double* az) {
 #pragma omp parallel for schedule(static) if (n > 256)

@@ -134,6 +134,17 @@ class Oracle(_Common):
     def num_threads(self) -> int:
         return int(self.lib.or_num_threads())
 
+    def time_sampled(self, x, y, z, m, G, eps, theta, ncrit, group_stride, quad=True):
+        """(build_ms, walk_ms, fraction_walked, pairs) of a sampled grouped walk on a full tree."""
+        x, y, z, m = map(_f64, (x, y, z, m))
+        out = np.zeros(4)
+        fn = self.lib.or_bh_time_sampled
+        fn.argtypes = [ctypes.c_int, _D, _D, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
+        if fn(len(x), _dp(x), _dp(y), _dp(z), _dp(m), G, eps, theta, ncrit, int(quad), int(group_stride), _dp(out)):
+            raise RuntimeError("or_bh_time_sampled failed")
+        return float(out[0]), float(out[1]), float(out[2]), float(out[3])
+
     def _tree_create(self, n, x, y, z, m, ncrit, max_depth, nn):
         return self.lib.or_tree_create(n, _dp(x), _dp(y), _dp(z), _dp(m), ncrit, max_depth, 1, nn)
 
@@ -240,6 +251,14 @@ class Reference(_Common):
         """The reference's own Plummer generator (mt19937; clips r at 20)."""
         arrs = [np.zeros(n) for _ in range(7)]
         self.lib.ref_plummer(n, seed, *[_dp(a) for a in arrs])
+        return arrs
+
+    def cloud(self, kind, n, seed):
+        """Input clouds of the reference self-tests: 'uniform' (BH vs Direct) or 'ball' (quadrupole)."""
+        arrs = [np.zeros(n) for _ in range(4)]
+        fn = self.lib.ref_cloud_uniform if kind == "uniform" else self.lib.ref_cloud_ball
+        fn.argtypes = [ctypes.c_int, ctypes.c_uint] + [_D] * 4
+        fn(n, seed, *[_dp(a) for a in arrs])
         return arrs
 
     def bh_accel(self, x, y, z, m, G, eps, theta, ncrit=8, quad=True, timed=False):

@@ -23,9 +23,12 @@
 #include "ngrav/Tree.hpp"
 #include "ngrav/ic/Plummer.hpp"
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <random>
 #include <vector>
 
 using namespace ngrav;
@@ -78,6 +81,35 @@ int ref_plummer(int n, unsigned seed, double* x, double* y, double* z, double* v
         m[i] = s.m[i];
     }
     return 0;
+}
+
+// Input cloud of the reference's BH-vs-Direct self-test (src/SelfTest.cpp:43-57):
+// uniform in [-1,1]^3, m = 0.5 + 0.5 (u + 1), std::mt19937(seed).
+void ref_cloud_uniform(int n, unsigned seed, double* x, double* y, double* z, double* m) {
+    std::mt19937 rng(seed);
+    std::uniform_real_distribution<double> u(-1.0, 1.0);
+    for (int i = 0; i < n; ++i) {
+        x[i] = u(rng);
+        y[i] = u(rng);
+        z[i] = u(rng);
+        m[i] = 0.5 + 0.5 * (u(rng) + 1.0);
+    }
+}
+
+// Input cloud of the reference's quadrupole self-test (src/SelfTest.cpp:212-227):
+// uniform in the unit ball (r = cbrt(u)), m = 1/n, std::mt19937(seed).
+void ref_cloud_ball(int n, unsigned seed, double* x, double* y, double* z, double* m) {
+    std::mt19937 rng(seed);
+    std::uniform_real_distribution<double> uni(0.0, 1.0);
+    for (int i = 0; i < n; ++i) {
+        const double r = std::cbrt(uni(rng));
+        const double cosT = 2.0 * uni(rng) - 1.0, sinT = std::sqrt(std::max(0.0, 1.0 - cosT * cosT));
+        const double phi = 2.0 * M_PI * uni(rng);
+        x[i] = r * sinT * std::cos(phi);
+        y[i] = r * sinT * std::sin(phi);
+        z[i] = r * cosT;
+        m[i] = 1.0 / n;
+    }
 }
 
 void ref_direct_accel(int n, const double* x, const double* y, const double* z, const double* m, double G,

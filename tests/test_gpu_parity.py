@@ -1,0 +1,150 @@
+"""CUDA path vs the reference (golden fixtures) and the oracle, through the C-ABI.
+
+Bars:
+  * keys, permutation (`order`) and tree topology: bit-exact;
+  * centres / half sizes: bit-exact (same FP64 recurrence);
+  * masses, COMs, maxRadius: FP64 on the GPU, relative 1e-12;
+  * quadrupoles: FP32 leaf sums, relative 1e-5 of the node's natural scale;
+  * accelerations vs the reference's CPU Barnes-Hut at the same theta:
+    median relative error <= 1e-5, max <= 1e-4 (FP32 evaluation).
+"""
+import numpy as np
+import pytest
+
+from conftest import TREE_EXACT, edge_cases, golden_tree, load_golden, octant_keys, rel_err
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ["split", "plain"]
+
+
+def make_sim(pkg, G, eps, theta, ncrit, precision="split", quad=True):
+    prec = pkg.PRECISION_SPLIT if precision == "split" else pkg.PRECISION_PLAIN
+    return pkg.NBodySystem(pkg.StepParams(G=G, eps=eps, theta=theta), leaf_capacity=ncrit, precision=prec,
+                           quadrupole=quad)
+
+
+def check_tree(sim, pkg, x, y, z, gold):
+    t = sim.debug_tree()
+    assert np.array_equal(t["keys"], octant_keys(x, y, z))
+    assert np.array_equal(t["order"], gold["order"])
+    c = pkg.canonical(t)
+    for k in TREE_EXACT:
+        assert np.array_equal(c[k], gold[k]), k
+    np.testing.assert_allclose(c["mass"], gold["mass"], rtol=1e-12)
+    np.testing.assert_allclose(c["com"], gold["com"], rtol=0, atol=1e-12 * max(1.0, np.abs(gold["com"]).max()))
+    np.testing.assert_allclose(c["max_radius"], gold["max_radius"], rtol=1e-12, atol=1e-14)
+    qs = gold["mass"][:, None] * gold["half"][:, None] ** 2
+    assert np.all(np.abs(c["quad"] - gold["quad"]) <= 1e-5 * qs + 1e-30)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_plummer16k_tree_bit_exact_and_accel(pkg, precision):
+    d = load_golden("plummer16k.npz")
+    x, y, z, m = d["x"], d["y"], d["z"], d["m"]
+    with make_sim(pkg, float(d["G"]), float(d["eps"]), float(d["theta"]), int(d["ncrit"]), precision) as sim:
+        sim.set_particles(x, y, z, d["vx"], d["vy"], d["vz"], m)
+        ax, ay, az = sim.compute_accel()
+        check_tree(sim, pkg, x, y, z, golden_tree(d))
+        st = sim.stats()
+    e = rel_err(ax, ay, az, d["ax"], d["ay"], d["az"])
+    assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (np.median(e), e.max())
+    assert st["groups"] == int(np.sum(d["tree_is_leaf"]))
+    assert st["depth_limited_leaves"] == 0 and st["status_bits"] == 0
+
+
+def test_plummer16k_interaction_counts_match_oracle(pkg, oracle):
+    d = load_golden("plummer16k.npz")
+    x, y, z, m = d["x"], d["y"], d["z"], d["m"]
+    _, _, _, cnt = oracle.bh_accel(x, y, z, m, 1.0, 0.01, 0.5, 16, counters=True)
+    with make_sim(pkg, 1.0, 0.01, 0.5, 16) as sim:
+        sim.set_particles(x, y, z, None, None, None, m)
+        sim.compute_accel()
+        st = sim.stats()
+    # Same opening decisions => the same interaction lists.
+    assert st["p2p_pairs"] == cnt["p2p_pairs"]
+    assert st["p2c_terms"] == cnt["p2c_terms"]
+    assert st["mac_tests"] == cnt["mac_tests"]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_selftest_theta0_vs_direct(pkg, precision):
+    """SelfTest.cpp:43-74 cloud: at theta 0 every node opens, BH == Direct
+    (the reference's 1e-12 bar is FP64; the FP32 bar here is 1e-5)."""
+    d = load_golden("selftest_uniform1000.npz")
+    x, y, z, m = d["x"], d["y"], d["z"], d["m"]
+    with make_sim(pkg, 1.0, 0.02, 0.0, 8, precision) as sim:
+        sim.set_particles(x, y, z, None, None, None, m)
+        ax, ay, az = sim.compute_accel()
+        check_tree(sim, pkg, x, y, z, golden_tree(d))
+    assert rel_err(ax, ay, az, d["dax"], d["day"], d["daz"]).max() <= 1e-5
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_selftest_quadrupole_gain(pkg, precision):
+    """SelfTest.cpp:212-265 cloud: quadrupole cuts the max error >= 3x."""
+    d = load_golden("selftest_ball4000.npz")
+    x, y, z, m = d["x"], d["y"], d["z"], d["m"]
+    errs = {}
+    for tag, quad in (("mono", False), ("quad", True)):
+        with make_sim(pkg, 1.0, 0.01, 0.5, 8, precision, quad=quad) as sim:
+            sim.set_particles(x, y, z, None, None, None, m)
+            ax, ay, az = sim.compute_accel()
+            if quad:
+                check_tree(sim, pkg, x, y, z, golden_tree(d))
+        e = rel_err(ax, ay, az, d[f"{tag}_ax"], d[f"{tag}_ay"], d[f"{tag}_az"])
+        assert np.median(e) <= 1e-5 and e.max() <= 1e-4
+        errs[tag] = rel_err(ax, ay, az, d["dax"], d["day"], d["daz"]).max()
+    assert errs["mono"] / errs["quad"] >= 3.0
+
+
+@pytest.mark.parametrize("name", edge_cases()[0])
+def test_edge_cases(pkg, name):
+    _, d = edge_cases()
+    x, y, z, m = (d[f"{name}_{k}"] for k in "xyzm")
+    ncrit = int(d[f"{name}_ncrit"])
+    gold = golden_tree(d, f"{name}_tree")
+    with make_sim(pkg, 1.0, 0.05, 0.5, ncrit) as sim:
+        sim.set_particles(x, y, z, None, None, None, m)
+        ax, ay, az = sim.compute_accel()
+        st = sim.stats()
+        if gold["level"].max() < 21:
+            check_tree(sim, pkg, x, y, z, gold)
+            assert st["depth_limited_leaves"] == 0
+        else:
+            assert st["depth_limited_leaves"] > 0
+    gx, gy, gz = d[f"{name}_ax"], d[f"{name}_ay"], d[f"{name}_az"]
+    if len(x) == 1:
+        assert ax[0] == 0.0 and ay[0] == 0.0 and az[0] == 0.0
+        return
+    e = rel_err(ax, ay, az, gx, gy, gz)
+    if gold["level"].max() < 21:
+        assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (np.median(e), e.max())
+    else:
+        assert np.median(e) <= 1e-3
+
+
+def test_determinism_bitwise(pkg, ic):
+    x, y, z, vx, vy, vz, m = ic.plummer(50000, seed=3)
+    outs = []
+    for _ in range(2):
+        with make_sim(pkg, 1.0, 0.01, 0.5, 16) as sim:
+            sim.set_particles(x, y, z, vx, vy, vz, m)
+            outs.append(np.stack(sim.compute_accel()))
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("n,ncrit", [(131072, 16), (65536, 8)])
+def test_medium_plummer_vs_oracle(pkg, oracle, ic, n, ncrit):
+    x, y, z, vx, vy, vz, m = (a.astype(np.float64) for a in ic.plummer(n, seed=11))
+    rx, ry, rz, cnt = oracle.bh_accel(x, y, z, m, 1.0, 0.005, 0.5, ncrit, counters=True)
+    with make_sim(pkg, 1.0, 0.005, 0.5, ncrit) as sim:
+        sim.set_particles(x, y, z, vx, vy, vz, m)
+        ax, ay, az = sim.compute_accel()
+        st = sim.stats()
+        t = sim.debug_tree()
+    ot = oracle.tree(x, y, z, m, ncrit)
+    assert np.array_equal(t["order"], ot["order"])
+    e = rel_err(ax, ay, az, rx, ry, rz)
+    assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (np.median(e), e.max())
+    assert st["p2p_pairs"] == cnt["p2p_pairs"] and st["p2c_terms"] == cnt["p2c_terms"]

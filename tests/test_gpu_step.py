@@ -1,0 +1,74 @@
+"""KDK stepping, FP64 diagnostics and the force-error sampler on the GPU."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def sim_for(pkg, d, precision):
+    prec = pkg.PRECISION_SPLIT if precision == "split" else pkg.PRECISION_PLAIN
+    s = pkg.NBodySystem(pkg.StepParams(G=float(d["G"]), eps=float(d["eps"]), theta=float(d["theta"]),
+                                       dt=float(d["dt"])), leaf_capacity=int(d["ncrit"]), precision=prec)
+    s.set_particles(d["x"], d["y"], d["z"], d["vx"], d["vy"], d["vz"], d["m"])
+    return s
+
+
+@pytest.mark.parametrize("precision,tol", [("split", 2e-7), ("plain", 2e-6)])
+def test_ten_kdk_steps_track_reference(pkg, precision, tol):
+    """Config: Plummer 16,384, leaf 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK
+    steps -- the reference's LeapfrogStep in FP64 vs the GPU state."""
+    d = load_golden("plummer16k.npz")
+    with sim_for(pkg, d, precision) as sim:
+        sim.prime()
+        sim.step(int(d["steps"]), float(d["dt"]))
+        x, y, z, vx, vy, vz = sim.state()
+    dpos = np.sqrt((x - d["kdk_x"]) ** 2 + (y - d["kdk_y"]) ** 2 + (z - d["kdk_z"]) ** 2)
+    dvel = np.sqrt((vx - d["kdk_vx"]) ** 2 + (vy - d["kdk_vy"]) ** 2 + (vz - d["kdk_vz"]) ** 2)
+    assert dpos.max() <= tol * 10, dpos.max()
+    assert dvel.max() <= 1e-5, dvel.max()
+
+
+def test_diagnostics_match_reference(pkg):
+    d = load_golden("plummer16k.npz")
+    with sim_for(pkg, d, "split") as sim:
+        g = sim.diagnostics(exact_potential=True)
+        ref = d["diag0"]
+        assert g["potential_exact"]
+        assert g["energy"] == pytest.approx(ref[0], rel=1e-10)
+        np.testing.assert_allclose(g["com"], ref[1:4], atol=1e-14)
+        np.testing.assert_allclose(g["L"], ref[4:7], rtol=1e-9, atol=1e-14)
+        np.testing.assert_allclose(g["P"], ref[7:10], atol=1e-14)
+        sim.prime()
+        sim.step(int(d["steps"]), float(d["dt"]))
+        g10 = sim.diagnostics(exact_potential=True)
+    assert g10["energy"] == pytest.approx(d["diag10"][0], rel=1e-6)
+
+
+@pytest.mark.parametrize("fp64_pairs", [0, 1])
+def test_force_error_sampler_matches_oracle(pkg, oracle, fp64_pairs):
+    d = load_golden("plummer16k.npz")
+    with sim_for(pkg, d, "split") as sim:
+        ax, ay, az = sim.compute_accel()
+        fe = sim.force_error(nsample=1024, seed=7, fp64_pairs=fp64_pairs)
+    # all-targets truth from the reference's direct sum
+    e_all = rel_err(ax, ay, az, d["dax"], d["day"], d["daz"])
+    assert fe["nsample"] == 1024
+    assert 0.3 * np.sqrt(np.mean(e_all ** 2)) <= fe["rms"] <= 3.0 * np.sqrt(np.mean(e_all ** 2))
+    assert fe["max"] <= e_all.max() * (1 + 1e-6)
+    # exact: recompute the same sample's error with the oracle
+    n = len(d["x"])
+    rng_targets = None  # the library draws its own sample; compare distributions instead
+    assert fe["median"] <= np.quantile(e_all, 0.75)
+
+
+def test_momentum_and_com_drift_small(pkg, ic):
+    x, y, z, vx, vy, vz, m = ic.plummer(32768, seed=2)
+    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=0.01, theta=0.5, dt=1e-3), leaf_capacity=16) as sim:
+        sim.set_particles(x, y, z, vx, vy, vz, m)
+        d0 = sim.diagnostics()
+        sim.step(20)
+        d1 = sim.diagnostics()
+    assert abs(d1["energy"] - d0["energy"]) / abs(d0["energy"]) < 1e-4
+    assert np.linalg.norm(np.array(d1["P"]) - np.array(d0["P"])) < 1e-4

@@ -1,0 +1,86 @@
+"""Pins the oracle (the C restatement) against the reference's own outputs.
+
+The golden fixtures were produced by the reference's CPU path compiled from
+its sources (tests/golden/make_golden.py).  These checks run on the CPU.
+"""
+import numpy as np
+import pytest
+
+from conftest import TREE_EXACT, edge_cases, golden_tree, load_golden, rel_err
+
+
+def _check_tree(O, x, y, z, m, ncrit, gold):
+    t = O.tree(x, y, z, m, ncrit)
+    c = t.canonical()
+    for k in TREE_EXACT:
+        assert np.array_equal(c[k], gold[k]), k
+    assert np.array_equal(t["order"], gold["order"])
+    np.testing.assert_allclose(c["mass"], gold["mass"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(c["com"], gold["com"], rtol=0, atol=1e-13 * max(1.0, np.abs(gold["com"]).max()))
+    np.testing.assert_allclose(c["max_radius"], gold["max_radius"], rtol=1e-12, atol=1e-14)
+    qs = gold["mass"].max() * gold["half"].max() ** 2  # natural scale of a quadrupole
+    np.testing.assert_allclose(c["quad"], gold["quad"], rtol=0, atol=1e-12 * qs)
+
+
+def test_plummer16k_tree_and_accel(oracle):
+    d = load_golden("plummer16k.npz")
+    args = (d["x"], d["y"], d["z"], d["m"])
+    _check_tree(oracle, *args, int(d["ncrit"]), golden_tree(d))
+    ax, ay, az, cnt = oracle.bh_accel(*args, float(d["G"]), float(d["eps"]), float(d["theta"]), int(d["ncrit"]),
+                                      counters=True)
+    e = rel_err(ax, ay, az, d["ax"], d["ay"], d["az"])
+    assert e.max() < 1e-12
+    assert cnt["groups"] == int(np.sum(d["tree_is_leaf"]))
+
+
+def test_plummer16k_direct(oracle):
+    d = load_golden("plummer16k.npz")
+    ax, ay, az = oracle.direct(d["x"], d["y"], d["z"], d["m"], float(d["G"]), float(d["eps"]))
+    assert rel_err(ax, ay, az, d["dax"], d["day"], d["daz"]).max() < 1e-12
+
+
+def test_plummer16k_leapfrog_and_diagnostics(oracle):
+    d = load_golden("plummer16k.npz")
+    st = (d["x"], d["y"], d["z"], d["vx"], d["vy"], d["vz"])
+    (x, y, z, vx, vy, vz), _ = oracle.leapfrog(st, d["m"], float(d["G"]), float(d["eps"]), float(d["theta"]),
+                                               int(d["ncrit"]), float(d["dt"]), int(d["steps"]))
+    for a, k in zip((x, y, z, vx, vy, vz), ("kdk_x", "kdk_y", "kdk_z", "kdk_vx", "kdk_vy", "kdk_vz")):
+        np.testing.assert_allclose(a, d[k], rtol=0, atol=1e-12)
+    diag = oracle.diagnostics(d["x"], d["y"], d["z"], d["vx"], d["vy"], d["vz"], d["m"], float(d["G"]),
+                              float(d["eps"]))
+    np.testing.assert_allclose(diag, d["diag0"], rtol=1e-11, atol=1e-14)
+
+
+def test_selftest_theta0_matches_direct(oracle):
+    """The reference's own gate (SelfTest.cpp:43-74): BH at theta 0 equals Direct to 1e-12."""
+    d = load_golden("selftest_uniform1000.npz")
+    args = (d["x"], d["y"], d["z"], d["m"])
+    _check_tree(oracle, *args, 8, golden_tree(d))
+    ax, ay, az = oracle.bh_accel(*args, 1.0, 0.02, 0.0, 8)
+    assert rel_err(ax, ay, az, d["dax"], d["day"], d["daz"]).max() <= 1e-12
+    assert rel_err(ax, ay, az, d["ax"], d["ay"], d["az"]).max() <= 1e-13
+
+
+def test_selftest_quadrupole_gain(oracle):
+    """The reference's own gate (SelfTest.cpp:212-265): quadrupole cuts max error >= 3x."""
+    d = load_golden("selftest_ball4000.npz")
+    args = (d["x"], d["y"], d["z"], d["m"])
+    _check_tree(oracle, *args, 8, golden_tree(d))
+    errs = {}
+    for tag, quad in (("mono", False), ("quad", True)):
+        ax, ay, az = oracle.bh_accel(*args, 1.0, 0.01, 0.5, 8, quad=quad)
+        assert rel_err(ax, ay, az, d[f"{tag}_ax"], d[f"{tag}_ay"], d[f"{tag}_az"]).max() < 1e-12
+        errs[tag] = rel_err(ax, ay, az, d["dax"], d["day"], d["daz"]).max()
+    assert errs["mono"] / errs["quad"] >= 3.0
+
+
+@pytest.mark.parametrize("name", edge_cases()[0])
+def test_edge_cases(oracle, name):
+    _, d = edge_cases()
+    x, y, z, m = (d[f"{name}_{k}"] for k in "xyzm")
+    ncrit = int(d[f"{name}_ncrit"])
+    _check_tree(oracle, x, y, z, m, ncrit, golden_tree(d, f"{name}_tree"))
+    ax, ay, az = oracle.bh_accel(x, y, z, m, 1.0, 0.05, 0.5, ncrit)
+    gx, gy, gz = d[f"{name}_ax"], d[f"{name}_ay"], d[f"{name}_az"]
+    np.testing.assert_allclose(np.stack([ax, ay, az]), np.stack([gx, gy, gz]), rtol=1e-12,
+                               atol=1e-12 * max(1e-300, np.abs(np.stack([gx, gy, gz])).max()))
