@@ -182,6 +182,28 @@ int ngrav_gpu_reset_cumulative(ngrav_gpu_ctx* ctx);
  * support.) */
 int ngrav_gpu_probe_fp32_peak(int device, double* tflops);
 
+/* Largest n ngrav_gpu_diagnostics_noalloc accepts: its block partials live in
+ * a fixed 256 KiB device array (4,096 blocks of 4,096 particles). */
+#define NGRAV_NOALLOC_MAX_N 16777216
+
+/* The conservation diagnostics of ngrav_gpu_diagnostics for callers that
+ * cannot allocate device memory -- e.g. a loop running under a framework's
+ * caching allocator that owns the device's memory, or one that must keep
+ * cudaMalloc/cudaFree (and cudaFree's device-wide synchronisation) out of
+ * its frame loop.  No reference counterpart.
+ *   x..m        caller-owned DEVICE arrays of n FP32 values on `device`
+ *   with_potential  1: also the exact O(N^2) FP64 pair potential (G, eps)
+ *   out         HOST struct, filled like ngrav_gpu_diagnostics fills it
+ * Allocates nothing: its scratch is a static 256 KiB device array that every
+ * GPU loading this library holds until exit.  The first call on a device
+ * looks that array's address up (so make it before any stream capture).
+ * Calls share the array, so calls overlapping on the GPU race; serialise
+ * them.  Runs on the legacy default stream and returns when done.
+ * Returns NGRAV_ERR_INVALID_ARG for n > NGRAV_NOALLOC_MAX_N. */
+int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const float* y, const float* z,
+                                  const float* vx, const float* vy, const float* vz, const float* m, double G,
+                                  double eps, int with_potential, ngrav_gpu_diag* out);
+
 /* Export the last tree for bit-exact checks.  Call with node arrays NULL to
  * get *nnodes; then call again with arrays of that size.
  *   keys[n]        63-bit octant-path key of each particle (original order)

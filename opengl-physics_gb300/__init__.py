@@ -40,8 +40,9 @@ EXPORTS = (
     "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
-    "ngrav_gpu_probe_fp32_peak",
+    "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
 )
+NOALLOC_MAX_N = 16777216
 
 
 class Opts(ctypes.Structure):
@@ -125,8 +126,24 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_debug_tree.argtypes = [ctypes.c_void_p, _I, _U64, _I, _I, _U64, _I, _I, _D, _D, _D, _D, _D, _D]
     L.ngrav_gpu_reset_cumulative.argtypes = [ctypes.c_void_p]
     L.ngrav_gpu_probe_fp32_peak.argtypes = [ctypes.c_int, _D]
+    L.ngrav_gpu_diagnostics_noalloc.argtypes = [ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 7 + \
+        [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Diag)]
     _lib = L
     return L
+
+
+def diagnostics_noalloc(device, n, x, y, z, vx, vy, vz, m, G, eps, with_potential=True):
+    """Conservation diagnostics of caller-owned device FP32 arrays (raw device
+    pointers as ints), allocating no device memory (see the C header)."""
+    L = load_library()
+    d = Diag()
+    rc = L.ngrav_gpu_diagnostics_noalloc(int(device), int(n), *[ctypes.c_void_p(int(p)) for p in
+                                                                (x, y, z, vx, vy, vz, m)],
+                                         float(G), float(eps), int(with_potential), ctypes.byref(d))
+    if rc != OK:
+        raise NgravError(rc, "ngrav_gpu_diagnostics_noalloc failed")
+    return dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
+                P=list(d.P), potential_exact=bool(d.potential_exact))
 
 
 def probe_fp32_peak(device: int = 0) -> float:
