@@ -15,8 +15,8 @@ e2e     = the same metric through the reference-facing C-ABI with host
           buffers: per step ngrav_gpu_set_particles_f32 from pinned host
           memory + ngrav_gpu_compute_accel into pinned FP64 host arrays
           (the ComputeAccelBarnesHut contract), wall clock.
-roofline: the walk kernel (P2P + P2C, FP32 pipe): algorithmic flops
-          (20 per P2P pair + 60 per P2C term, device-counted) / its
+roofline: the evaluation kernel (P2P + P2C, FP32 pipe): algorithmic
+          flops (20 per P2P pair + 60 per P2C term, device-counted) / its
           event-timed duration, against the measured FP32 FMA peak.
 cpu_baseline: the oracle (C restatement of the reference's CPU path) on the
           host cores, bounded sample: full tree build + walk over every
@@ -213,8 +213,8 @@ def main():
 
     # roofline of the walk kernel
     flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
-    walk_s = st["cum_ms_walk"] * 1e-3
-    achieved = flops / walk_s / 1e12 if walk_s > 0 else None
+    force_s = st["cum_ms_force"] * 1e-3
+    achieved = flops / force_s / 1e12 if force_s > 0 else None
     peak = pkg.probe_fp32_peak(dev)
     force = sim.force_error(nsample=4096, seed=2024, fp64_pairs=False)
 
@@ -273,10 +273,12 @@ def main():
                        "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
                        "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
                        "ms_walk_per_step": st["cum_ms_walk"] / max(1, st["cum_evals"]),
+                       "ms_force_per_step": st["cum_ms_force"] / max(1, st["cum_evals"]),
+                       "list_entries_per_step": st["far_entries"] + st["near_entries"],
                        "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"])},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
-                         "kernel": "walk_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
+                         "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
                          "peak_source": "measured FP32 FMA probe (ngrav_gpu_probe_fp32_peak)"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,
         }

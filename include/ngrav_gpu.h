@@ -95,7 +95,7 @@ typedef struct ngrav_gpu_ferr {
 
 typedef struct ngrav_gpu_stats {
     /* last force evaluation (milliseconds; 0 unless opts.timing) */
-    double ms_bbox_keys, ms_sort, ms_build, ms_moments, ms_walk, ms_kick, ms_total;
+    double ms_bbox_keys, ms_sort, ms_build, ms_moments, ms_walk, ms_force, ms_total;
     /* interaction counts of the last force evaluation (device counters) */
     long long p2p_pairs;   /* softened particle-particle terms (self excluded) */
     long long p2c_terms;   /* far-node terms */
@@ -112,10 +112,14 @@ typedef struct ngrav_gpu_stats {
      * context's stream; the per-phase ones need opts.timing) */
     long long cum_evals;
     long long cum_p2p_pairs, cum_p2c_terms;
-    double cum_ms_walk;    /* walk kernel (P2P + P2C + closing kick) */
+    double cum_ms_walk;    /* tree walk kernel (opening tests, interaction lists) */
+    double cum_ms_force;   /* evaluation kernel (P2P + P2C + closing kick) */
     double cum_ms_eval;    /* whole force evaluations */
     double cum_ms_step;    /* ngrav_gpu_step calls, first to last kernel */
     long long cum_launches; /* kernels this context launched */
+    /* interaction lists of the last evaluation */
+    long long far_entries, near_entries;
+    int list_max;          /* longest per-group list */
 } ngrav_gpu_stats;
 
 typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;

@@ -66,7 +66,7 @@ class Ferr(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("ms_bbox_keys", ctypes.c_double), ("ms_sort", ctypes.c_double), ("ms_build", ctypes.c_double),
-                ("ms_moments", ctypes.c_double), ("ms_walk", ctypes.c_double), ("ms_kick", ctypes.c_double),
+                ("ms_moments", ctypes.c_double), ("ms_walk", ctypes.c_double), ("ms_force", ctypes.c_double),
                 ("ms_total", ctypes.c_double), ("p2p_pairs", ctypes.c_longlong), ("p2c_terms", ctypes.c_longlong),
                 ("mac_tests", ctypes.c_longlong), ("mac_retests", ctypes.c_longlong), ("groups", ctypes.c_longlong),
                 ("nodes", ctypes.c_int), ("leaves", ctypes.c_int), ("levels", ctypes.c_int),
@@ -74,8 +74,9 @@ class Stats(ctypes.Structure):
                 ("walk_stack_max", ctypes.c_int), ("status_bits", ctypes.c_uint), ("force_evals", ctypes.c_longlong),
                 ("n", ctypes.c_longlong), ("cum_evals", ctypes.c_longlong), ("cum_p2p_pairs", ctypes.c_longlong),
                 ("cum_p2c_terms", ctypes.c_longlong), ("cum_ms_walk", ctypes.c_double),
-                ("cum_ms_eval", ctypes.c_double), ("cum_ms_step", ctypes.c_double),
-                ("cum_launches", ctypes.c_longlong)]
+                ("cum_ms_force", ctypes.c_double), ("cum_ms_eval", ctypes.c_double),
+                ("cum_ms_step", ctypes.c_double), ("cum_launches", ctypes.c_longlong),
+                ("far_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong), ("list_max", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -42,9 +42,9 @@ struct ngrav_gpu_ctx {
     unsigned* flags = nullptr;
     unsigned* scanbuf = nullptr;
     int* leaf_list = nullptr;
-    int* stack_pool = nullptr;
-    int stack_cap = 0;
-    int nwarps = 0;
+    ListBuffers LB;
+    int eval_nwarps = 0;
+    long long gi_cap = 0;
     double* stage = nullptr;          // 7 * cap_n doubles (upload / download staging)
     double* dpartial = nullptr;
     long long dpartial_cap = 0;
@@ -63,7 +63,7 @@ struct ngrav_gpu_ctx {
     // cumulative measurement counters (ngrav_gpu_reset_cumulative)
     long long launches = 0;
     long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
-    double cum_ms_walk = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
+    double cum_ms_walk = 0.0, cum_ms_force = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
 };
 
 namespace {
@@ -185,9 +185,39 @@ int initial_node_cap(long long n, int leaf_cap) {
 }
 
 int alloc_stack(ngrav_gpu_ctx* ctx, int stack_cap) {
-    dfree(ctx->stack_pool);
-    NG_CUDA(dalloc(ctx->stack_pool, (long long)ctx->nwarps * stack_cap));
-    ctx->stack_cap = stack_cap;
+    dfree(ctx->LB.stack);
+    NG_CUDA(dalloc(ctx->LB.stack, (long long)ctx->LB.nwarps * stack_cap));
+    ctx->LB.stack_cap = stack_cap;
+    return NGRAV_OK;
+}
+
+int alloc_scratch(ngrav_gpu_ctx* ctx, int scratch_cap) {
+    dfree(ctx->LB.scratch);
+    NG_CUDA(dalloc(ctx->LB.scratch, 2LL * ctx->LB.nwarps * scratch_cap));
+    ctx->LB.scratch_cap = scratch_cap;
+    return NGRAV_OK;
+}
+
+int alloc_lists(ngrav_gpu_ctx* ctx, long long far_cap, long long near_cap) {
+    ListBuffers& L = ctx->LB;
+    if (far_cap > L.far_cap) {
+        dfree(L.far);
+        NG_CUDA(dalloc(L.far, far_cap));
+        L.far_cap = far_cap;
+    }
+    if (near_cap > L.near_cap) {
+        dfree(L.near);
+        NG_CUDA(dalloc(L.near, near_cap));
+        L.near_cap = near_cap;
+    }
+    return NGRAV_OK;
+}
+
+int alloc_group_info(ngrav_gpu_ctx* ctx, long long n) {
+    dfree(ctx->LB.goff);
+    dfree(ctx->LB.gcnt);
+    NG_CUDA(dalloc(ctx->LB.goff, 2 * std::max<long long>(n, 1)));
+    NG_CUDA(dalloc(ctx->LB.gcnt, 2 * std::max<long long>(n, 1)));
     return NGRAV_OK;
 }
 
@@ -205,7 +235,7 @@ WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
     wp.retest = o.fp64_mac_retest ? 1 : 0;
     wp.kick = kick ? 1 : 0;
     wp.hdt = hdt;
-    wp.stack_cap = ctx->stack_cap;
+    wp.stack_cap = ctx->LB.stack_cap;
     wp.node_limit = ctx->T.cap + 32;
     return wp;
 }
@@ -249,9 +279,12 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     launch_moments(ctx->T, ctx->C, P, ctx->leaf_list, n, (int)std::min<long long>(n, ctx->T.cap), split,
                    ctx->opts.quadrupole != 0, s);
     rec(ctx, 4);
-    launch_walk(ctx->T, ctx->C, P, ctx->leaf_list, (int)n, walk_params(ctx, kick, hdt), ctx->stack_pool,
-                ctx->nwarps, s);
+    const WalkParams wp = walk_params(ctx, kick, hdt);
+    launch_walk(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, s);
     rec(ctx, 5);
+    launch_eval(ctx->T, ctx->C, P, ctx->leaf_list, wp, ctx->LB, ctx->eval_nwarps, s);
+    rec(ctx, 6);
+    ctx->launches += 1;  // the evaluation kernel
 }
 
 int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
@@ -269,23 +302,44 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
         retry = true;
         return NGRAV_OK;
     }
+    if (st & kStCorrupt) return fail(ctx, NGRAV_ERR_CAPACITY, "walk visit limit breached (inconsistent tree)");
     if (st & kStStackOverflow) {
-        if (ctx->stack_cap >= (1 << 22)) return fail(ctx, NGRAV_ERR_CAPACITY, "walk stack exhausted");
-        NG_TRY(alloc_stack(ctx, ctx->stack_cap * 2));
+        if (ctx->LB.stack_cap >= (1 << 22)) return fail(ctx, NGRAV_ERR_CAPACITY, "walk stack exhausted");
+        NG_TRY(alloc_stack(ctx, ctx->LB.stack_cap * 2));
         retry = true;
         return NGRAV_OK;
+    }
+    if (st & kStListOverflow) {
+        const long long ft = (long long)ctx->hc.far_total, nt = (long long)ctx->hc.near_total;
+        const bool pool = ft > ctx->LB.far_cap || nt > ctx->LB.near_cap;
+        if (pool) {
+            NG_TRY(alloc_lists(ctx, std::max(ctx->LB.far_cap * 2, ft + ft / 2),
+                               std::max(ctx->LB.near_cap * 2, nt + nt / 2)));
+        } else {
+            if (ctx->LB.scratch_cap >= (1 << 24)) return fail(ctx, NGRAV_ERR_CAPACITY, "list staging exhausted");
+            NG_TRY(alloc_scratch(ctx, ctx->LB.scratch_cap * 2));
+        }
+        retry = true;
+        return NGRAV_OK;
+    }
+    // Keep headroom in the list pools for the next evaluation.
+    {
+        const long long ft = (long long)ctx->hc.far_total, nt = (long long)ctx->hc.near_total;
+        if (ft > ctx->LB.far_cap - ctx->LB.far_cap / 8 || nt > ctx->LB.near_cap - ctx->LB.near_cap / 8)
+            NG_TRY(alloc_lists(ctx, std::max(ctx->LB.far_cap, ft + ft / 4), std::max(ctx->LB.near_cap, nt + nt / 4)));
     }
     if (ctx->opts.strict_depth && ctx->hc.depth_limited > 0)
         return fail(ctx, NGRAV_ERR_DEPTH, "a leaf needs more than 21 key levels");
     if (ctx->events) {
         float ms;
-        for (int i = 0; i < 5; ++i) {
+        for (int i = 0; i < 6; ++i) {
             cudaEventElapsedTime(&ms, ctx->ev[i], ctx->ev[i + 1]);
             ctx->phase_ms[i] = ms;
         }
         ctx->cum_ms_walk += ctx->phase_ms[4];
+        ctx->cum_ms_force += ctx->phase_ms[5];
         ctx->cum_ms_eval += ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] +
-                            ctx->phase_ms[4];
+                            ctx->phase_ms[4] + ctx->phase_ms[5];
     }
     ctx->force_evals += 1;
     ctx->cum_evals += 1;
@@ -336,6 +390,11 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
     NG_TRY(alloc_particles(ctx, std::max<int64_t>(n, 1)));
     if (ctx->T.cap < initial_node_cap(n, ctx->opts.leaf_capacity))
         NG_TRY(alloc_nodes(ctx, initial_node_cap(n, ctx->opts.leaf_capacity)));
+    if (ctx->cap_n > 0 && (ctx->LB.goff == nullptr || n > ctx->gi_cap)) {
+        NG_TRY(alloc_group_info(ctx, ctx->cap_n));
+        ctx->gi_cap = ctx->cap_n;
+    }
+    NG_TRY(alloc_lists(ctx, 64 * std::max<long long>(n, 1) + 4096, 16 * std::max<long long>(n, 1) + 4096));
     ctx->n = n;
     if (n > 0) {
         T* st = reinterpret_cast<T*>(ctx->stage);
@@ -404,8 +463,13 @@ int ngrav_gpu_create(ngrav_gpu_ctx** out, const ngrav_gpu_opts* opts) {
         NG_CUDA(cudaMalloc((void**)&ctx->C, sizeof(Counters)));
         walk_set_attributes();
         NG_CUDA(cudaGetLastError());
-        ctx->nwarps = ctx->sm_count * walk_blocks_per_sm() * walk_warps_per_block();
+        // Walk: up to 32 resident warps per SM (latency-bound traversal);
+        // evaluation: every warp the occupancy calculator allows.
+        ctx->LB.nwarps = ctx->sm_count * std::min(walk_blocks_per_sm(), 32 / walk_warps_per_block()) *
+                         walk_warps_per_block();
+        ctx->eval_nwarps = ctx->sm_count * eval_blocks_per_sm() * eval_warps_per_block();
         NG_TRY(alloc_stack(ctx, 4096));
+        NG_TRY(alloc_scratch(ctx, 8192));
         for (int i = 0; i < 8; ++i) NG_CUDA(cudaEventCreate(&ctx->ev[i]));
         for (int i = 0; i < 2; ++i) NG_CUDA(cudaEventCreate(&ctx->sev[i]));
         ctx->events = ctx->opts.timing != 0;
@@ -428,7 +492,12 @@ void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
     free_particles(ctx);
     free_nodes(ctx);
     dfree(ctx->C);
-    dfree(ctx->stack_pool);
+    dfree(ctx->LB.stack);
+    dfree(ctx->LB.scratch);
+    dfree(ctx->LB.far);
+    dfree(ctx->LB.near);
+    dfree(ctx->LB.goff);
+    dfree(ctx->LB.gcnt);
     dfree(ctx->dpartial);
     dfree(ctx->dtargets);
     dfree(ctx->dslots);
@@ -676,7 +745,9 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->ms_build = ctx->phase_ms[2];
     out->ms_moments = ctx->phase_ms[3];
     out->ms_walk = ctx->phase_ms[4];
-    out->ms_total = ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] + ctx->phase_ms[4];
+    out->ms_force = ctx->phase_ms[5];
+    out->ms_total = ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] + ctx->phase_ms[4] +
+                    ctx->phase_ms[5];
     out->p2p_pairs = (long long)c.p2p_pairs;
     out->p2c_terms = (long long)c.p2c_terms;
     out->mac_tests = (long long)c.mac_tests;
@@ -695,6 +766,10 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->cum_p2p_pairs = ctx->cum_pairs;
     out->cum_p2c_terms = ctx->cum_p2c;
     out->cum_ms_walk = ctx->cum_ms_walk;
+    out->cum_ms_force = ctx->cum_ms_force;
+    out->far_entries = (long long)c.far_total;
+    out->near_entries = (long long)c.near_total;
+    out->list_max = c.list_max;
     out->cum_ms_eval = ctx->cum_ms_eval;
     out->cum_ms_step = ctx->cum_ms_step;
     out->cum_launches = ctx->launches;
@@ -705,7 +780,7 @@ int ngrav_gpu_reset_cumulative(ngrav_gpu_ctx* ctx) {
     if (!ctx) return NGRAV_ERR_INVALID_ARG;
     ctx->launches = 0;
     ctx->cum_evals = ctx->cum_pairs = ctx->cum_p2c = 0;
-    ctx->cum_ms_walk = ctx->cum_ms_eval = ctx->cum_ms_step = 0.0;
+    ctx->cum_ms_walk = ctx->cum_ms_force = ctx->cum_ms_eval = ctx->cum_ms_step = 0.0;
     return NGRAV_OK;
 }
 

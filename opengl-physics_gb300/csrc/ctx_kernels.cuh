@@ -23,11 +23,12 @@ void launch_potential(long long n, const Particles& P, bool split, double eps2, 
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
                     bool fp64_pairs, double* out, cudaStream_t s);
 void launch_reset_counters(Counters* C, cudaStream_t s);
-int walk_blocks_for(int nwarps);
-size_t walk_smem_bytes();
 void walk_set_attributes();
 int walk_warps_per_block();
 int walk_blocks_per_sm();
+int eval_warps_per_block();
+int eval_blocks_per_sm();
+size_t eval_smem_bytes();
 void launch_gather_slots(const int* inv, const int* targets, int nt, int* slots, cudaStream_t s);
 double run_fma_probe(int sm_count, cudaStream_t s);
 

@@ -31,7 +31,9 @@ enum : unsigned {
     kStDepthLimit = 4u,     // warning: a depth-21 leaf holds more than leaf_capacity
     kStNonFinite = 8u,
     kStTimeout = 16u,
-    kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout,
+    kStListOverflow = 32u,  // per-warp list staging or the final list pool
+    kStCorrupt = 64u,       // walk visit limit breached
+    kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout | kStListOverflow | kStCorrupt,
 };
 
 // Per-evaluation device counters (zeroed before each force evaluation).
@@ -50,12 +52,30 @@ struct Counters {
     int nleaves;
     int max_leaf_count;
     int depth_limited;
-    int work_next;                    // dynamic group scheduler
+    int work_next;                    // dynamic group scheduler (walk)
     int stack_max;
     int levels_used;
-    int pad;
+    int eval_next;                    // dynamic group scheduler (evaluation)
     double root_center[3];
     double root_half;
+    unsigned long long far_total;     // interaction-list allocators
+    unsigned long long near_total;
+    int list_max;                     // longest per-group list seen
+    int pad2;
+};
+
+// Per-group interaction lists written by the walk, read by the evaluation.
+struct ListBuffers {
+    long long far_cap = 0, near_cap = 0;
+    int* far = nullptr;               // far node ids, contiguous per group
+    int* near = nullptr;              // near leaf ids, contiguous per group
+    long long* goff = nullptr;        // per group: far offset, near offset
+    int* gcnt = nullptr;              // per group: far count, near count
+    int* scratch = nullptr;           // per walking warp: far then near staging
+    int scratch_cap = 0;              // entries per list per warp
+    int* stack = nullptr;             // per walking warp traversal stack
+    int stack_cap = 0;
+    int nwarps = 0;                   // resident walking warps
 };
 
 struct NodeArrays {
@@ -80,8 +100,8 @@ struct NodeArrays {
     // FP32 walk records
     float4* wA = nullptr;             // com_hi.xyz, mass
     float4* wB = nullptr;             // Qxx, Qyy, Qxy, Qxz
-    float4* wC = nullptr;             // Qyz, 2h, link (int bits), meta (int bits)
-    float4* wD = nullptr;             // com_lo.xyz, maxR (leaves, rounded up)
+    float4* wC = nullptr;             // maxR (rounded up), 2h, link (int bits), meta (int bits)
+    float4* wD = nullptr;             // com_lo.xyz, Qyz
     float4* chi = nullptr;            // centre hi (leaves; SPLIT)
     float4* clo = nullptr;            // centre lo (leaves; SPLIT)
 };
@@ -153,8 +173,10 @@ void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, uns
                       int* leaf_list, SortBuffers& sb, cudaStream_t s);
 void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,
                     int max_leaves, bool split, bool quadrupole, cudaStream_t s);
-void launch_walk(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, int max_leaves,
-                 const WalkParams& wp, int* stack_pool, int nwarps, cudaStream_t s);
+void launch_walk(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
+                 const ListBuffers& LB, cudaStream_t s);
+void launch_eval(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, const WalkParams& wp,
+                 const ListBuffers& LB, int nwarps, cudaStream_t s);
 void launch_kick_drift(const Particles& P, long long n, float hdt, float dt, bool split, Counters* C,
                        cudaStream_t s);
 void launch_scatter_accel(const Particles& P, long long n, double* ax, double* ay, double* az, cudaStream_t s);

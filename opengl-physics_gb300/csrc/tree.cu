@@ -202,10 +202,10 @@ __device__ __forceinline__ void write_walk_record(NodeArrays& T, int node, doubl
     T.wA[node] = make_float4(hx, hy, hz, (float)M);
     T.wB[node] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
     const double size = 2.0 * ldexp(root_half, -level);
-    T.wC[node] = make_float4((float)Q[4], (float)size, __int_as_float(link),
+    T.wC[node] = make_float4(round_up_f(maxr), (float)size, __int_as_float(link),
                              __int_as_float(meta_pack(leaf, cnt_or_nch, level)));
     T.wD[node] = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy), (float)(cz - (double)hz),
-                             round_up_f(maxr));
+                             (float)Q[4]);
 }
 
 __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C, const float4* __restrict__ pos,
