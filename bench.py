@@ -45,6 +45,7 @@ import __graft_entry__ as ge  # noqa: E402
 WORKLOADS = {
     # name: (generator, kwargs, eps, dt, theta, leaf capacity)
     "galaxy4m": ("galaxy", {}, 0.002, 2e-4, 0.6, 16),
+    "galaxy1m": ("galaxy", {"n_halo": 943718, "n_disk": 104858}, 0.002, 2e-4, 0.6, 16),
     "plummer1m": ("plummer", {"n": 1048576, "seed": 1}, 0.005, 5e-4, 0.5, 16),
     "plummer16k": ("plummer", {"n": 16384, "seed": 0}, 0.01, 1e-3, 0.5, 16),
 }
@@ -275,6 +276,10 @@ def main():
                        "ms_walk_per_step": st["cum_ms_walk"] / max(1, st["cum_evals"]),
                        "ms_force_per_step": st["cum_ms_force"] / max(1, st["cum_evals"]),
                        "list_entries_per_step": st["far_entries"] + st["near_entries"],
+                       "mac_tests_per_step": st["mac_tests"], "mac_retests_per_step": st["mac_retests"],
+                       "walk_stack_max": st["walk_stack_max"], "leaves": st["leaves"], "nodes": st["nodes"],
+                       "ms_phases_last_eval": {k: st[k] for k in ("ms_bbox_keys", "ms_sort", "ms_build",
+                                                                  "ms_moments", "ms_walk", "ms_force")},
                        "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"])},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved and peak else None, "traffic": None,

@@ -45,6 +45,7 @@ struct ngrav_gpu_ctx {
     ListBuffers LB;
     int eval_nwarps = 0;
     long long gi_cap = 0;
+    bool walk_global_stack = false;
     double* stage = nullptr;          // 7 * cap_n doubles (upload / download staging)
     double* dpartial = nullptr;
     long long dpartial_cap = 0;
@@ -191,33 +192,31 @@ int alloc_stack(ngrav_gpu_ctx* ctx, int stack_cap) {
     return NGRAV_OK;
 }
 
-int alloc_scratch(ngrav_gpu_ctx* ctx, int scratch_cap) {
-    dfree(ctx->LB.scratch);
-    NG_CUDA(dalloc(ctx->LB.scratch, 2LL * ctx->LB.nwarps * scratch_cap));
-    ctx->LB.scratch_cap = scratch_cap;
-    return NGRAV_OK;
-}
-
-int alloc_lists(ngrav_gpu_ctx* ctx, long long far_cap, long long near_cap) {
+// Grow the chunk pools of the interaction lists (chunks of kListChunk ids).
+int alloc_lists(ngrav_gpu_ctx* ctx, long long far_chunks, long long near_chunks) {
     ListBuffers& L = ctx->LB;
-    if (far_cap > L.far_cap) {
+    far_chunks = std::min<long long>(far_chunks, 0x7FFFFFF0LL);
+    near_chunks = std::min<long long>(near_chunks, 0x7FFFFFF0LL);
+    if (far_chunks > L.far_chunk_cap) {
         dfree(L.far);
-        NG_CUDA(dalloc(L.far, far_cap));
-        L.far_cap = far_cap;
+        dfree(L.far_next);
+        NG_CUDA(dalloc(L.far, far_chunks * kListChunk));
+        NG_CUDA(dalloc(L.far_next, far_chunks));
+        L.far_chunk_cap = (int)far_chunks;
     }
-    if (near_cap > L.near_cap) {
+    if (near_chunks > L.near_chunk_cap) {
         dfree(L.near);
-        NG_CUDA(dalloc(L.near, near_cap));
-        L.near_cap = near_cap;
+        dfree(L.near_next);
+        NG_CUDA(dalloc(L.near, near_chunks * kListChunk));
+        NG_CUDA(dalloc(L.near_next, near_chunks));
+        L.near_chunk_cap = (int)near_chunks;
     }
     return NGRAV_OK;
 }
 
 int alloc_group_info(ngrav_gpu_ctx* ctx, long long n) {
-    dfree(ctx->LB.goff);
-    dfree(ctx->LB.gcnt);
-    NG_CUDA(dalloc(ctx->LB.goff, 2 * std::max<long long>(n, 1)));
-    NG_CUDA(dalloc(ctx->LB.gcnt, 2 * std::max<long long>(n, 1)));
+    dfree(ctx->LB.ginfo);
+    NG_CUDA(dalloc(ctx->LB.ginfo, std::max<long long>(n, 1)));
     return NGRAV_OK;
 }
 
@@ -237,6 +236,7 @@ WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
     wp.hdt = hdt;
     wp.stack_cap = ctx->LB.stack_cap;
     wp.node_limit = ctx->T.cap + 32;
+    wp.global_stack = ctx->walk_global_stack ? 1 : 0;
     return wp;
 }
 
@@ -304,29 +304,31 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
     }
     if (st & kStCorrupt) return fail(ctx, NGRAV_ERR_CAPACITY, "walk visit limit breached (inconsistent tree)");
     if (st & kStStackOverflow) {
-        if (ctx->LB.stack_cap >= (1 << 22)) return fail(ctx, NGRAV_ERR_CAPACITY, "walk stack exhausted");
-        NG_TRY(alloc_stack(ctx, ctx->LB.stack_cap * 2));
+        if (!ctx->walk_global_stack) {
+            ctx->walk_global_stack = true;  // the shared-memory stack was too small for this tree
+        } else {
+            if (ctx->LB.stack_cap >= (1 << 22)) return fail(ctx, NGRAV_ERR_CAPACITY, "walk stack exhausted");
+            NG_TRY(alloc_stack(ctx, ctx->LB.stack_cap * 2));
+        }
         retry = true;
         return NGRAV_OK;
     }
     if (st & kStListOverflow) {
-        const long long ft = (long long)ctx->hc.far_total, nt = (long long)ctx->hc.near_total;
-        const bool pool = ft > ctx->LB.far_cap || nt > ctx->LB.near_cap;
-        if (pool) {
-            NG_TRY(alloc_lists(ctx, std::max(ctx->LB.far_cap * 2, ft + ft / 2),
-                               std::max(ctx->LB.near_cap * 2, nt + nt / 2)));
-        } else {
-            if (ctx->LB.scratch_cap >= (1 << 24)) return fail(ctx, NGRAV_ERR_CAPACITY, "list staging exhausted");
-            NG_TRY(alloc_scratch(ctx, ctx->LB.scratch_cap * 2));
-        }
+        // The walk kept counting chunks past the pool: size the pools to that
+        // (plus headroom) and run again.
+        const long long fc = (long long)(unsigned)ctx->hc.far_chunks, nc = (long long)(unsigned)ctx->hc.near_chunks;
+        if (fc >= 0x7FFFFFF0LL || nc >= 0x7FFFFFF0LL) return fail(ctx, NGRAV_ERR_CAPACITY, "list pool exhausted");
+        NG_TRY(alloc_lists(ctx, fc + fc / 4 + 1024, nc + nc / 4 + 1024));
         retry = true;
         return NGRAV_OK;
     }
     // Keep headroom in the list pools for the next evaluation.
     {
-        const long long ft = (long long)ctx->hc.far_total, nt = (long long)ctx->hc.near_total;
-        if (ft > ctx->LB.far_cap - ctx->LB.far_cap / 8 || nt > ctx->LB.near_cap - ctx->LB.near_cap / 8)
-            NG_TRY(alloc_lists(ctx, std::max(ctx->LB.far_cap, ft + ft / 4), std::max(ctx->LB.near_cap, nt + nt / 4)));
+        const long long fc = ctx->hc.far_chunks, nc = ctx->hc.near_chunks;
+        if (fc > ctx->LB.far_chunk_cap - ctx->LB.far_chunk_cap / 8 ||
+            nc > ctx->LB.near_chunk_cap - ctx->LB.near_chunk_cap / 8)
+            NG_TRY(alloc_lists(ctx, std::max<long long>(ctx->LB.far_chunk_cap, fc + fc / 4),
+                               std::max<long long>(ctx->LB.near_chunk_cap, nc + nc / 4)));
     }
     if (ctx->opts.strict_depth && ctx->hc.depth_limited > 0)
         return fail(ctx, NGRAV_ERR_DEPTH, "a leaf needs more than 21 key levels");
@@ -390,11 +392,15 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
     NG_TRY(alloc_particles(ctx, std::max<int64_t>(n, 1)));
     if (ctx->T.cap < initial_node_cap(n, ctx->opts.leaf_capacity))
         NG_TRY(alloc_nodes(ctx, initial_node_cap(n, ctx->opts.leaf_capacity)));
-    if (ctx->cap_n > 0 && (ctx->LB.goff == nullptr || n > ctx->gi_cap)) {
+    if (ctx->cap_n > 0 && (ctx->LB.ginfo == nullptr || n > ctx->gi_cap)) {
         NG_TRY(alloc_group_info(ctx, ctx->cap_n));
         ctx->gi_cap = ctx->cap_n;
     }
-    NG_TRY(alloc_lists(ctx, 64 * std::max<long long>(n, 1) + 4096, 16 * std::max<long long>(n, 1) + 4096));
+    // Initial pools: a few chunks per leaf group; the first evaluation sizes them.
+    {
+        const long long groups = std::max<long long>(n, 1) / std::max(1, ctx->opts.leaf_capacity / 2) + 1;
+        NG_TRY(alloc_lists(ctx, 4 * groups + 1024, 2 * groups + 1024));
+    }
     ctx->n = n;
     if (n > 0) {
         T* st = reinterpret_cast<T*>(ctx->stage);
@@ -461,7 +467,7 @@ int ngrav_gpu_create(ngrav_gpu_ctx** out, const ngrav_gpu_opts* opts) {
         NG_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->opts.device));
         NG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         NG_CUDA(cudaMalloc((void**)&ctx->C, sizeof(Counters)));
-        walk_set_attributes();
+        eval_set_attributes();
         NG_CUDA(cudaGetLastError());
         // Walk: up to 32 resident warps per SM (latency-bound traversal);
         // evaluation: every warp the occupancy calculator allows.
@@ -469,7 +475,6 @@ int ngrav_gpu_create(ngrav_gpu_ctx** out, const ngrav_gpu_opts* opts) {
                          walk_warps_per_block();
         ctx->eval_nwarps = ctx->sm_count * eval_blocks_per_sm() * eval_warps_per_block();
         NG_TRY(alloc_stack(ctx, 4096));
-        NG_TRY(alloc_scratch(ctx, 8192));
         for (int i = 0; i < 8; ++i) NG_CUDA(cudaEventCreate(&ctx->ev[i]));
         for (int i = 0; i < 2; ++i) NG_CUDA(cudaEventCreate(&ctx->sev[i]));
         ctx->events = ctx->opts.timing != 0;
@@ -493,11 +498,11 @@ void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
     free_nodes(ctx);
     dfree(ctx->C);
     dfree(ctx->LB.stack);
-    dfree(ctx->LB.scratch);
     dfree(ctx->LB.far);
     dfree(ctx->LB.near);
-    dfree(ctx->LB.goff);
-    dfree(ctx->LB.gcnt);
+    dfree(ctx->LB.far_next);
+    dfree(ctx->LB.near_next);
+    dfree(ctx->LB.ginfo);
     dfree(ctx->dpartial);
     dfree(ctx->dtargets);
     dfree(ctx->dslots);
@@ -767,8 +772,8 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->cum_p2c_terms = ctx->cum_p2c;
     out->cum_ms_walk = ctx->cum_ms_walk;
     out->cum_ms_force = ctx->cum_ms_force;
-    out->far_entries = (long long)c.far_total;
-    out->near_entries = (long long)c.near_total;
+    out->far_entries = (long long)c.far_chunks * kListChunk;
+    out->near_entries = (long long)c.near_chunks * kListChunk;
     out->list_max = c.list_max;
     out->cum_ms_eval = ctx->cum_ms_eval;
     out->cum_ms_step = ctx->cum_ms_step;

@@ -23,7 +23,7 @@ void launch_potential(long long n, const Particles& P, bool split, double eps2, 
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
                     bool fp64_pairs, double* out, cudaStream_t s);
 void launch_reset_counters(Counters* C, cudaStream_t s);
-void walk_set_attributes();
+void eval_set_attributes();
 int walk_warps_per_block();
 int walk_blocks_per_sm();
 int eval_warps_per_block();

@@ -58,21 +58,25 @@ struct Counters {
     int eval_next;                    // dynamic group scheduler (evaluation)
     double root_center[3];
     double root_half;
-    unsigned long long far_total;     // interaction-list allocators
+    unsigned long long far_total;     // list entries written (far, near)
     unsigned long long near_total;
     int list_max;                     // longest per-group list seen
+    int far_chunks;                   // chunk allocators (may exceed the pool: then
+    int near_chunks;                  //   they count what a retry needs)
     int pad2;
 };
 
 // Per-group interaction lists written by the walk, read by the evaluation.
+// Each list is a chain of kListChunk-entry chunks taken from a pool with one
+// atomic per chunk; next[c] links chunk c to the following one.
+constexpr int kListChunk = 128;
 struct ListBuffers {
-    long long far_cap = 0, near_cap = 0;
-    int* far = nullptr;               // far node ids, contiguous per group
-    int* near = nullptr;              // near leaf ids, contiguous per group
-    long long* goff = nullptr;        // per group: far offset, near offset
-    int* gcnt = nullptr;              // per group: far count, near count
-    int* scratch = nullptr;           // per walking warp: far then near staging
-    int scratch_cap = 0;              // entries per list per warp
+    int far_chunk_cap = 0, near_chunk_cap = 0;
+    int* far = nullptr;               // far node ids, far_chunk_cap * kListChunk
+    int* near = nullptr;              // near leaf ids
+    int* far_next = nullptr;          // chunk links
+    int* near_next = nullptr;
+    int4* ginfo = nullptr;            // per group: far first chunk, near first chunk, far count, near count
     int* stack = nullptr;             // per walking warp traversal stack
     int stack_cap = 0;
     int nwarps = 0;                   // resident walking warps
@@ -154,6 +158,7 @@ struct WalkParams {
     float hdt;
     int stack_cap;
     int node_limit;                   // visits per group beyond this mean a corrupt tree
+    int global_stack;                 // walk stack in global memory (fallback for deep frontiers)
 };
 
 // ---- launchers (each enqueues on `s`; no host synchronisation) ----

@@ -1,0 +1,521 @@
+// eval.cu -- force evaluation from the walk's interaction lists: P2C over
+// each group's far list, P2P over its near list, and the closing half-kick.
+//
+// Arithmetic restates the reference (projects/nbody_core/src/Solvers.cpp):
+//   P2P  a += G m d / (|d|^2 + eps^2)^(3/2)                 (AccumPairPlummer, :19-38)
+//   P2C  the same softened monopole of the node's mass at its COM, plus the
+//        unsoftened traceless quadrupole
+//        a += -G Q.d / r^5 + 2.5 G (d.Q.d) d / r^7       (AddQuadrupole, :147-179)
+// with the group's own members included as a near leaf (the self term is
+// zero for eps > 0 and masked for eps == 0).
+//
+// GB300 mapping.  One warp per group (dynamic scheduling), lane = (target t,
+// slice s): nt targets x floor(32/nt) source slices, slices summed at the end
+// of the group.  Far records are staged 32 at a time into shared memory in
+// the group's frame, the next batch loading into registers while this one is
+// evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
+// per leaf, completing on an mbarrier with a bounded wait) into two
+// alternating shared-memory buffers: batch k+1 copies in while batch k is
+// evaluated.  In SPLIT precision each lane's partial sums are Kahan
+// compensated once per staged chunk.
+#include "engine.cuh"
+
+namespace ngrav {
+
+constexpr int kEvalWarps = 4;
+constexpr int kEvalThreads = kEvalWarps * 32;
+constexpr int kSrcCap = 256;                  // sources per staging buffer (4 KiB)
+constexpr int kBuffers = 1;                   // staging buffers per warp (2 halves occupancy)
+constexpr unsigned kWaitLimit = 1u << 26;     // bounded mbarrier polling
+
+struct __align__(128) EvalSmem {
+    float4 src[kBuffers][kSrcCap];            // TMA destinations
+    float4 farA[32];                          // far batch: COM in the group frame, mass
+    float4 farB[32];                          //   Qxx Qyy Qxy Qxz
+    float farQ[32];                           //   Qyz
+    float red[3][32];                         // slice reduction
+    float4 shift[kBuffers][32];               // near-leaf frame shift (SPLIT)
+    int start[kBuffers][32];
+    int cnt[kBuffers][32];
+    int pre[kBuffers][33];
+    unsigned long long bar[2];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait for the phase with parity `phase`; false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase) {
+    const unsigned b = smem_u32(bar);
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ int excl_scan(int v, int lane, int& total) {
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+// Lane mapping for a block of nt <= 32 targets: lane = (target t, slice s),
+// t = lane % nt, s = lane / nt, S = floor(32 / nt) slices; slice s handles
+// sources s, s + S, s + 2S, ...  All lanes of a slice read the same source
+// (shared-memory broadcast); consecutive slices read consecutive sources.
+struct Lane {
+    float tx, ty, tz;
+    int sl, S, nt;
+    bool active;
+    float ax, ay, az, cx, cy, cz;
+};
+
+// Adds one chunk's partial sum; in SPLIT precision Kahan-compensated (the
+// compensation costs four adds per component per chunk, not per pair).
+template <bool SPLIT>
+__device__ __forceinline__ void accumulate(Lane& g, float px, float py, float pz) {
+    if (SPLIT) {
+        float y = px - g.cx, t = g.ax + y;
+        g.cx = (t - g.ax) - y;
+        g.ax = t;
+        y = py - g.cy;
+        t = g.ay + y;
+        g.cy = (t - g.ay) - y;
+        g.ay = t;
+        y = pz - g.cz;
+        t = g.az + y;
+        g.cz = (t - g.az) - y;
+        g.az = t;
+    } else {
+        g.ax += px;
+        g.ay += py;
+        g.az += pz;
+    }
+}
+
+template <bool SPLIT, bool ZEROSOFT>
+__device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_src, int ns, float eps2) {
+    if (!g.active) return;
+    float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+    const float tx = g.tx, ty = g.ty, tz = g.tz;
+    const int S = g.S;
+    int j = g.sl;
+    for (; j + S < ns; j += 2 * S) {  // two independent chains per lane
+        const float4 a = s_src[j];
+        const float4 b = s_src[j + S];
+        const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
+        const float bx_ = b.x - tx, by_ = b.y - ty, bz_ = b.z - tz;
+        const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
+        const float rb = fmaf(bx_, bx_, fmaf(by_, by_, fmaf(bz_, bz_, eps2)));
+        const float ia = rsqrtf(ra), ib = rsqrtf(rb);
+        float fa = a.w * (ia * ia * ia), fb = b.w * (ib * ib * ib);
+        if (ZEROSOFT) {
+            fa = ra > 0.f ? fa : 0.f;
+            fb = rb > 0.f ? fb : 0.f;
+        }
+        px = fmaf(fa, ax_, px);
+        py = fmaf(fa, ay_, py);
+        pz = fmaf(fa, az_, pz);
+        qx = fmaf(fb, bx_, qx);
+        qy = fmaf(fb, by_, qy);
+        qz = fmaf(fb, bz_, qz);
+    }
+    if (j < ns) {
+        const float4 a = s_src[j];
+        const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
+        const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
+        const float ia = rsqrtf(ra);
+        float fa = a.w * (ia * ia * ia);
+        if (ZEROSOFT) fa = ra > 0.f ? fa : 0.f;
+        px = fmaf(fa, ax_, px);
+        py = fmaf(fa, ay_, py);
+        pz = fmaf(fa, az_, pz);
+    }
+    accumulate<SPLIT>(g, px + qx, py + qy, pz + qz);
+}
+
+template <bool SPLIT, bool QUAD>
+__device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA, const float4* __restrict__ fB,
+                                          const float* __restrict__ fQ, int nf, float eps2) {
+    if (!g.active) return;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    const float tx = g.tx, ty = g.ty, tz = g.tz;
+    for (int f = g.sl; f < nf; f += g.S) {
+        const float4 A = fA[f];
+        const float dx = A.x - tx, dy = A.y - ty, dz = A.z - tz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float rs = rsqrtf(r2 + eps2);
+        const float fm = A.w * (rs * rs * rs);
+        px = fmaf(fm, dx, px);
+        py = fmaf(fm, dy, py);
+        pz = fmaf(fm, dz, pz);
+        if (QUAD) {
+            const float4 B = fB[f];
+            const float qyz = fQ[f];
+            const float qzz = -(B.x + B.y);
+            const float qdx = fmaf(B.x, dx, fmaf(B.z, dy, B.w * dz));
+            const float qdy = fmaf(B.z, dx, fmaf(B.y, dy, qyz * dz));
+            const float qdz = fmaf(B.w, dx, fmaf(qyz, dy, qzz * dz));
+            const float qd2 = fmaf(dx, qdx, fmaf(dy, qdy, dz * qdz));
+            const float ir = rsqrtf(r2);
+            const float ir2 = ir * ir;
+            const float ir5 = ir2 * ir2 * ir;
+            const float c2 = 2.5f * qd2 * (ir5 * ir2);
+            px = fmaf(-ir5, qdx, fmaf(c2, dx, px));
+            py = fmaf(-ir5, qdy, fmaf(c2, dy, py));
+            pz = fmaf(-ir5, qdz, fmaf(c2, dz, pz));
+        }
+    }
+    accumulate<SPLIT>(g, px, py, pz);
+}
+
+// One near batch's info, loaded into registers by lanes e < be.
+struct NearInfo {
+    int start, cnt;
+    float4 shift;
+};
+
+template <bool SPLIT>
+__device__ __forceinline__ NearInfo load_near_info(const NodeArrays& T, const ListBuffers& LB, int chunk, int idx,
+                                                   bool valid, const float4& gchi, const float4& gclo) {
+    NearInfo r;
+    r.start = 0;
+    r.cnt = 0;
+    r.shift = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) {
+        const int node = LB.near[(long long)chunk * kListChunk + (idx & (kListChunk - 1))];
+        const float4 Cw = T.wC[node];
+        r.start = __float_as_int(Cw.z);
+        r.cnt = __float_as_int(Cw.w) & 0xFFFFFF;
+        if (SPLIT) {
+            const float4 h = T.chi[node], l = T.clo[node];
+            r.shift = make_float4((h.x - gchi.x) + (l.x - gclo.x), (h.y - gchi.y) + (l.y - gclo.y),
+                                  (h.z - gchi.z) + (l.z - gclo.z), 0.f);
+        }
+    }
+    return r;
+}
+
+// Publish a batch's info to buffer `b` and start its TMA copies; returns the
+// number of staged sources.
+__device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& in, int lane,
+                                          const float4* __restrict__ src) {
+    int tot;
+    const int ex = excl_scan(in.cnt, lane, tot);
+    sm.start[b][lane] = in.start;
+    sm.cnt[b][lane] = in.cnt;
+    sm.pre[b][lane] = ex;
+    if (lane == 31) sm.pre[b][32] = tot;
+    sm.shift[b][lane] = in.shift;
+    if (tot > 0) {
+        if (lane == 0) mbar_expect_tx(&sm.bar[b], (unsigned)tot * 16u);
+        __syncwarp();
+        if (in.cnt > 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tma_load_1d(&sm.src[b][ex], src + in.start, (unsigned)in.cnt * 16u, &sm.bar[b]);
+        }
+    }
+    __syncwarp();
+    return tot;
+}
+
+template <bool SPLIT, bool QUAD, bool ZEROSOFT>
+__global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counters* C,
+                                                            const float4* __restrict__ src,
+                                                            float4* __restrict__ acc, float4* __restrict__ vel,
+                                                            const int* __restrict__ leaf_list, WalkParams wp,
+                                                            ListBuffers LB) {
+    extern __shared__ __align__(128) unsigned char eval_smem_raw[];
+    const int lane = threadIdx.x & 31;
+    EvalSmem& sm = reinterpret_cast<EvalSmem*>(eval_smem_raw)[threadIdx.x >> 5];
+    if (C->status & kStFatal) return;
+    if (lane == 0) {
+        mbar_init(&sm.bar[0]);
+        mbar_init(&sm.bar[1]);
+    }
+    __syncwarp();
+    unsigned phase[2] = {0u, 0u};
+    const int nleaves = C->nleaves;
+    // Leaves per near batch: the largest power of two whose worst-case
+    // source count fits one staging buffer (so a batch never straddles a
+    // 128-entry list chunk).
+    const int maxleaf = max(1, C->max_leaf_count);
+    int be = 1;
+    while (be < 32 && (be * 2) * maxleaf <= kSrcCap) be *= 2;
+    const bool big_leaves = maxleaf > kSrcCap;
+    unsigned long long pairs = 0, p2c = 0;
+    bool timeout = false;
+
+    for (;;) {
+        int gi = 0;
+        if (lane == 0) gi = atomicAdd(&C->eval_next, 1);
+        gi = __shfl_sync(0xffffffffu, gi, 0);
+        if (gi >= nleaves) break;
+        const int leaf = leaf_list[gi];
+        const float4 gC = T.wC[leaf];
+        const int gstart = __float_as_int(gC.z);
+        const int gcount = __float_as_int(gC.w) & 0xFFFFFF;
+        const int4 gin = LB.ginfo[gi];
+        const int far_first = gin.x, near_first = gin.y, nfar = gin.z, nnear = gin.w;
+        float4 gchi = make_float4(0.f, 0.f, 0.f, 0.f), gclo = gchi;
+        if (SPLIT) {
+            gchi = T.chi[leaf];
+            gclo = T.clo[leaf];
+        }
+        for (int t0 = 0; t0 < gcount; t0 += 32) {
+            Lane g;
+            g.nt = min(32, gcount - t0);
+            g.S = 32 / g.nt;
+            g.active = lane < g.nt * g.S;
+            g.sl = lane / g.nt;
+            const float4 tp = src[gstart + t0 + lane % g.nt];
+            g.tx = tp.x;
+            g.ty = tp.y;
+            g.tz = tp.z;
+            g.ax = g.ay = g.az = g.cx = g.cy = g.cz = 0.f;
+
+            // ---- far field: batches of 32 records; the next batch loads while this one computes ----
+            {
+                int c = far_first;
+                float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, D = A;
+                if (lane < nfar) {
+                    const int node = LB.far[(long long)c * kListChunk + lane];
+                    A = T.wA[node];
+                    D = T.wD[node];
+                    if (QUAD) B = T.wB[node];
+                }
+                for (int b = 0; b < nfar; b += 32) {
+                    if (b + lane < nfar) {
+                        float4 rA = A;
+                        if (SPLIT) {
+                            rA.x = (A.x - gchi.x) + (D.x - gclo.x);
+                            rA.y = (A.y - gchi.y) + (D.y - gclo.y);
+                            rA.z = (A.z - gchi.z) + (D.z - gclo.z);
+                        }
+                        sm.farA[lane] = rA;
+                        if (QUAD) {
+                            sm.farB[lane] = B;
+                            sm.farQ[lane] = D.w;
+                        }
+                    }
+                    __syncwarp();
+                    const int nb = b + 32;
+                    if (nb < nfar) {
+                        if ((nb & (kListChunk - 1)) == 0) c = LB.far_next[c];
+                        if (nb + lane < nfar) {
+                            const int node = LB.far[(long long)c * kListChunk + (nb & (kListChunk - 1)) + lane];
+                            A = T.wA[node];
+                            D = T.wD[node];
+                            if (QUAD) B = T.wB[node];
+                        }
+                    }
+                    p2c_chunk<SPLIT, QUAD>(g, sm.farA, sm.farB, sm.farQ, min(32, nfar - b), wp.eps2);
+                    __syncwarp();
+                }
+            }
+            p2c += (unsigned long long)g.nt * (unsigned long long)nfar;
+
+            // ---- near field: batches of `be` leaves staged by TMA, double-buffered ----
+            int total = 0;
+            if (!big_leaves) {
+                const int nbatch = (nnear + be - 1) / be;
+                int chunk_pf = near_first;  // list chunk of the batch being prefetched
+                NearInfo info = load_near_info<SPLIT>(T, LB, chunk_pf, lane, lane < be && lane < nnear, gchi, gclo);
+                int ns_cur = stage_batch(sm, 0, info, lane, src);
+                if (nbatch > 1) {
+                    const int i1 = be;
+                    if ((i1 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
+                    info = load_near_info<SPLIT>(T, LB, chunk_pf, i1 + lane, lane < be && i1 + lane < nnear, gchi,
+                                                 gclo);
+                }
+                for (int k = 0; k < nbatch; ++k) {
+                    const int bcur = kBuffers == 2 ? (k & 1) : 0;
+                    int ns_next = 0;
+                    if (kBuffers == 2 && k + 1 < nbatch) {
+                        ns_next = stage_batch(sm, bcur ^ 1, info, lane, src);
+                        const int i2 = (k + 2) * be;
+                        if (k + 2 < nbatch) {
+                            if ((i2 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
+                            info = load_near_info<SPLIT>(T, LB, chunk_pf, i2 + lane, lane < be && i2 + lane < nnear,
+                                                         gchi, gclo);
+                        }
+                    }
+                    if (ns_cur > 0) {
+                        if (!mbar_wait(&sm.bar[bcur], phase[bcur])) {
+                            timeout = true;
+                            break;
+                        }
+                        phase[bcur] ^= 1u;
+                        if (SPLIT && lane < be) {  // move staged sources into the group's frame
+                            const float4 sh = sm.shift[bcur][lane];
+                            float4* q = &sm.src[bcur][sm.pre[bcur][lane]];
+                            for (int kk = 0; kk < sm.cnt[bcur][lane]; ++kk) {
+                                float4 v = q[kk];
+                                v.x += sh.x;
+                                v.y += sh.y;
+                                v.z += sh.z;
+                                q[kk] = v;
+                            }
+                        }
+                        __syncwarp();
+                        p2p_chunk<SPLIT, ZEROSOFT>(g, sm.src[bcur], ns_cur, wp.eps2);
+                        __syncwarp();
+                    }
+                    total += ns_cur;
+                    if (kBuffers == 1 && k + 1 < nbatch) {
+                        // single buffer: stage the next batch (its info is in
+                        // registers) and fetch the info of the one after
+                        ns_next = stage_batch(sm, 0, info, lane, src);
+                        const int i2 = (k + 2) * be;
+                        if (k + 2 < nbatch) {
+                            if ((i2 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
+                            info = load_near_info<SPLIT>(T, LB, chunk_pf, i2 + lane, lane < be && i2 + lane < nnear,
+                                                         gchi, gclo);
+                        }
+                    }
+                    ns_cur = ns_next;
+                }
+                if (timeout) {
+                    // give copies still in flight a bounded chance to land
+                    mbar_wait(&sm.bar[0], phase[0]);
+                    if (kBuffers == 2) mbar_wait(&sm.bar[1], phase[1]);
+                }
+            } else {
+                // Leaves larger than a staging buffer (depth-limited): plain loads, piecewise.
+                int c = near_first;
+                for (int b = 0; b < nnear; ++b) {
+                    if (b > 0 && (b & (kListChunk - 1)) == 0) c = LB.near_next[c];
+                    const int node = LB.near[(long long)c * kListChunk + (b & (kListChunk - 1))];
+                    const float4 Cw = T.wC[node];
+                    const int st = __float_as_int(Cw.z), cn = __float_as_int(Cw.w) & 0xFFFFFF;
+                    float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (SPLIT) {
+                        const float4 h = T.chi[node], l = T.clo[node];
+                        sh = make_float4((h.x - gchi.x) + (l.x - gclo.x), (h.y - gchi.y) + (l.y - gclo.y),
+                                         (h.z - gchi.z) + (l.z - gclo.z), 0.f);
+                    }
+                    for (int off = 0; off < cn; off += kSrcCap) {
+                        const int ns = min(kSrcCap, cn - off);
+                        __syncwarp();
+                        for (int j = lane; j < ns; j += 32) {
+                            float4 v = src[st + off + j];
+                            v.x += sh.x;
+                            v.y += sh.y;
+                            v.z += sh.z;
+                            sm.src[0][j] = v;
+                        }
+                        __syncwarp();
+                        p2p_chunk<SPLIT, ZEROSOFT>(g, sm.src[0], ns, wp.eps2);
+                    }
+                    __syncwarp();
+                    total += cn;
+                }
+            }
+            if (timeout) break;
+            pairs += (unsigned long long)g.nt * (unsigned long long)total - (unsigned long long)g.nt;
+
+            // ---- sum the slices of each target, write a, closing kick ----
+            if (g.active) {
+                sm.red[0][lane] = g.ax;
+                sm.red[1][lane] = g.ay;
+                sm.red[2][lane] = g.az;
+            }
+            __syncwarp();
+            if (lane < g.nt) {
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+                for (int s = 0; s < g.S; ++s) {
+                    sx += sm.red[0][lane + s * g.nt];
+                    sy += sm.red[1][lane + s * g.nt];
+                    sz += sm.red[2][lane + s * g.nt];
+                }
+                const float ax = wp.G * sx, ay = wp.G * sy, az = wp.G * sz;
+                const int slot = gstart + t0 + lane;
+                acc[slot] = make_float4(ax, ay, az, 0.f);
+                if (wp.kick) {
+                    float4 v = vel[slot];
+                    v.x = fmaf(wp.hdt, ax, v.x);
+                    v.y = fmaf(wp.hdt, ay, v.y);
+                    v.z = fmaf(wp.hdt, az, v.z);
+                    vel[slot] = v;
+                }
+            }
+            __syncwarp();
+        }
+        if (timeout) break;
+    }
+    if (timeout && lane == 0) atomicOr(&C->status, kStTimeout);
+    if (lane == 0) {
+        atomicAdd(&C->p2p_pairs, pairs);
+        atomicAdd(&C->p2c_terms, p2c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+size_t eval_smem_bytes() { return sizeof(EvalSmem) * kEvalWarps; }
+int eval_warps_per_block() { return kEvalWarps; }
+
+#define NGRAV_EVAL_INSTANCES(X) \
+    X(true, true, true) X(true, true, false) X(true, false, true) X(true, false, false) \
+    X(false, true, true) X(false, true, false) X(false, false, true) X(false, false, false)
+
+void eval_set_attributes() {
+    const int bytes = (int)eval_smem_bytes();
+#define NGRAV_ATTR(SP, Q, Z) \
+    cudaFuncSetAttribute(eval_kernel<SP, Q, Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    NGRAV_EVAL_INSTANCES(NGRAV_ATTR)
+#undef NGRAV_ATTR
+}
+
+int eval_blocks_per_sm() {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_kernel<true, true, false>, kEvalThreads,
+                                                  eval_smem_bytes());
+    return nb > 0 ? nb : 1;
+}
+
+void launch_eval(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, const WalkParams& wp,
+                 const ListBuffers& LB, int nwarps, cudaStream_t s) {
+    const int blocks = (nwarps + kEvalWarps - 1) / kEvalWarps;
+    const bool zs = !(wp.eps2 > 0.f);
+    const size_t smem = eval_smem_bytes();
+#define NGRAV_LAUNCH(SP, Q, Z)                                                                             \
+    if (wp.split == (SP) && (wp.quadrupole != 0) == (Q) && zs == (Z))                                     \
+        eval_kernel<SP, Q, Z><<<blocks, kEvalThreads, smem, s>>>(T, C, P.src, P.acc, P.vel, leaf_list, wp, LB);
+    NGRAV_EVAL_INSTANCES(NGRAV_LAUNCH)
+#undef NGRAV_LAUNCH
+}
+
+}  // namespace ngrav
