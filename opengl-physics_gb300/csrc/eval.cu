@@ -14,10 +14,12 @@
 // of the group.  Far records are staged 32 at a time into shared memory in
 // the group's frame, the next batch loading into registers while this one is
 // evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
-// per leaf, completing on an mbarrier with a bounded wait) into two
-// alternating shared-memory buffers: batch k+1 copies in while batch k is
-// evaluated.  In SPLIT precision each lane's partial sums are Kahan
-// compensated once per staged chunk.
+// per leaf, completing on an mbarrier with a bounded wait) into a 4 KiB
+// shared-memory buffer, batches of leaves sized by the leaf capacity; the
+// next batch's leaf records load while a batch is in flight.  (A second
+// buffer would overlap copy and compute within the warp, but halves the
+// resident warps; measured slower.)  In SPLIT precision each lane's partial
+// sums are Kahan compensated once per staged chunk.
 #include "engine.cuh"
 
 namespace ngrav {
