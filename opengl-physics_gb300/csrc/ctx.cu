@@ -264,8 +264,9 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     radix_sort_pairs(ctx->SB, n, passes, s);
     launch_permute(P, ctx->SB.vals, n, split, s);
     // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,
-    // tree init, 21 levels, leaf list (mark, 3 scan kernels, compact), moments, walk
-    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + kKeyLevels + 5 + 1 + 1;
+    // tree init, 21 levels, leaf list (mark, 3 scan kernels, compact), leaf
+    // moments, 21 internal-moment levels, walk
+    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + kKeyLevels + 5 + 1 + kKeyLevels + 1;
     std::swap(P.pos, P.pos2);
     std::swap(P.plo, P.plo2);
     std::swap(P.vel, P.vel2);
@@ -851,7 +852,29 @@ int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* o
     NG_TRY(get3(center, ctx->T.cx, ctx->T.cy, ctx->T.cz));
     NG_TRY(get3(com, ctx->T.comx, ctx->T.comy, ctx->T.comz));
     if (mass) NG_CUDA(cudaMemcpy(mass, ctx->T.mass, sizeof(double) * nn, cudaMemcpyDeviceToHost));
-    if (max_radius) NG_CUDA(cudaMemcpy(max_radius, ctx->T.maxr, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+    if (max_radius) {
+        // Leaves carry maxRadius from the device; internal nodes take the
+        // reference's upsweep, max over children of maxR_c + |com_c - com|
+        // (Tree.cpp:193-201), here on the host from the exported arrays.
+        NG_CUDA(cudaMemcpy(max_radius, ctx->T.maxr, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+        std::vector<double> cm(3 * (size_t)nn);
+        NG_TRY(get3(cm.data(), ctx->T.comx, ctx->T.comy, ctx->T.comz));
+        std::vector<unsigned char> nch(nn);
+        NG_CUDA(cudaMemcpy(nch.data(), ctx->T.nchild, nn, cudaMemcpyDeviceToHost));
+        std::vector<int> by_level(nn);
+        for (int v = 0; v < nn; ++v) by_level[v] = v;
+        std::stable_sort(by_level.begin(), by_level.end(), [&](int a, int b) { return lv[a] > lv[b]; });
+        for (int v : by_level) {
+            if (fc[v] == -1) continue;
+            double r = 0.0;
+            for (int c = fc[v]; c < fc[v] + nch[v]; ++c) {
+                const double dx = cm[3 * c] - cm[3 * v], dy = cm[3 * c + 1] - cm[3 * v + 1],
+                             dz = cm[3 * c + 2] - cm[3 * v + 2];
+                r = std::max(r, max_radius[c] + std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            max_radius[v] = r;
+        }
+    }
     if (quad) NG_CUDA(cudaMemcpy(quad, ctx->T.quad, sizeof(double) * 5 * nn, cudaMemcpyDeviceToHost));
     return NGRAV_OK;
 }

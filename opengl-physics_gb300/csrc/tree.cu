@@ -235,9 +235,10 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         const double ccx = T.cx[leaf], ccy = T.cy[leaf], ccz = T.cz[leaf];
         double cx = ccx, cy = ccy, cz = ccz;
         if (M > 0.0) {
-            cx = Sx / M;
-            cy = Sy / M;
-            cz = Sz / M;
+            const double inv = 1.0 / M;
+            cx = Sx * inv;
+            cy = Sy * inv;
+            cz = Sz * inv;
         }
         double maxr2 = 0.0;
         float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f, q4 = 0.f;
@@ -275,58 +276,57 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         const float hx = (float)ccx, hy = (float)ccy, hz = (float)ccz;
         T.chi[leaf] = make_float4(hx, hy, hz, 0.f);
         T.clo[leaf] = make_float4((float)(ccx - (double)hx), (float)(ccy - (double)hy), (float)(ccz - (double)hz), 0.f);
+    }
+}
 
-        // Climb while this thread is the last child to arrive.
-        int node = leaf;
-        for (;;) {
-            const int parent = T.parent[node];
-            if (parent < 0) break;
-            __threadfence();
-            const int nch = T.nchild[parent];
-            const int old = atomicAdd(&T.visit[parent], 1);
-            if (old != nch - 1) break;
-            __threadfence();
-            const int fc = T.first_child[parent];
-            double PM = 0.0, px = 0.0, py = 0.0, pz = 0.0;
-            for (int c = fc; c < fc + nch; ++c) {
-                const double mc = __ldcg(T.mass + c);
-                PM += mc;
-                px = fma(mc, __ldcg(T.comx + c), px);
-                py = fma(mc, __ldcg(T.comy + c), py);
-                pz = fma(mc, __ldcg(T.comz + c), pz);
-            }
-            double pcx = T.cx[parent], pcy = T.cy[parent], pcz = T.cz[parent];
-            if (PM > 0.0) {
-                pcx = px / PM;
-                pcy = py / PM;
-                pcz = pz / PM;
-            }
-            double PQ[5] = {0, 0, 0, 0, 0};
-            double pr = 0.0;
-            for (int c = fc; c < fc + nch; ++c) {
-                const double mc = __ldcg(T.mass + c);
-                const double dx = __ldcg(T.comx + c) - pcx, dy = __ldcg(T.comy + c) - pcy,
-                             dz = __ldcg(T.comz + c) - pcz;
-                const double d2 = dx * dx + dy * dy + dz * dz;
-                pr = fmax(pr, __ldcg(T.maxr + c) + sqrt(d2));
-                if (mc <= 0.0) continue;
-                if (quadrupole) {
-                    PQ[0] += __ldcg(T.quad + 5 * c + 0) + mc * (3.0 * dx * dx - d2);
-                    PQ[1] += __ldcg(T.quad + 5 * c + 1) + mc * (3.0 * dy * dy - d2);
-                    PQ[2] += __ldcg(T.quad + 5 * c + 2) + mc * 3.0 * dx * dy;
-                    PQ[3] += __ldcg(T.quad + 5 * c + 3) + mc * 3.0 * dx * dz;
-                    PQ[4] += __ldcg(T.quad + 5 * c + 4) + mc * 3.0 * dy * dz;
-                }
-            }
-            T.mass[parent] = PM;
-            T.comx[parent] = pcx;
-            T.comy[parent] = pcy;
-            T.comz[parent] = pcz;
-            T.maxr[parent] = pr;
-            for (int k = 0; k < 5; ++k) T.quad[5 * parent + k] = PQ[k];
-            write_walk_record(T, parent, PM, pcx, pcy, pcz, PQ, pr, false, fc, nch, T.level[parent], root_half);
-            node = parent;
+// Internal nodes of one level, from their (finished) children, in FP64: mass,
+// COM (sum m x / M), traceless quadrupole by the parallel-axis shift
+// (Tree.cpp:235-251).  maxRadius of internal nodes is not needed by the
+// walk (only leaves are groups); the tree export derives it on the host.
+__global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, const Counters* __restrict__ C, int l,
+                                                              int quadrupole) {
+    const int begin = C->level_begin[l];
+    const int end = C->level_begin[l + 1];
+    const double root_half = C->root_half;
+    for (int node = begin + blockIdx.x * blockDim.x + threadIdx.x; node < end; node += gridDim.x * blockDim.x) {
+        const int fc = T.first_child[node];
+        if (fc < 0) continue;
+        const int nch = T.nchild[node];
+        double PM = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+        for (int c = fc; c < fc + nch; ++c) {
+            const double mc = T.mass[c];
+            PM += mc;
+            px = fma(mc, T.comx[c], px);
+            py = fma(mc, T.comy[c], py);
+            pz = fma(mc, T.comz[c], pz);
         }
+        double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
+        if (PM > 0.0) {
+            const double inv = 1.0 / PM;
+            pcx = px * inv;
+            pcy = py * inv;
+            pcz = pz * inv;
+        }
+        double PQ[5] = {0, 0, 0, 0, 0};
+        if (quadrupole) {
+            for (int c = fc; c < fc + nch; ++c) {
+                const double mc = T.mass[c];
+                if (mc <= 0.0) continue;
+                const double dx = T.comx[c] - pcx, dy = T.comy[c] - pcy, dz = T.comz[c] - pcz;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                PQ[0] += T.quad[5 * c + 0] + mc * (3.0 * dx * dx - d2);
+                PQ[1] += T.quad[5 * c + 1] + mc * (3.0 * dy * dy - d2);
+                PQ[2] += T.quad[5 * c + 2] + mc * 3.0 * dx * dy;
+                PQ[3] += T.quad[5 * c + 3] + mc * 3.0 * dx * dz;
+                PQ[4] += T.quad[5 * c + 4] + mc * 3.0 * dy * dz;
+            }
+        }
+        T.mass[node] = PM;
+        T.comx[node] = pcx;
+        T.comy[node] = pcy;
+        T.comz[node] = pcz;
+        for (int k = 0; k < 5; ++k) T.quad[5 * node + k] = PQ[k];
+        write_walk_record(T, node, PM, pcx, pcy, pcz, PQ, 0.0, false, fc, nch, l, root_half);
     }
 }
 
@@ -337,6 +337,11 @@ void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* l
     if (blocks < 1) blocks = 1;
     moments_kernel<<<(unsigned)blocks, 128, 0, s>>>(T, C, P.pos, split ? P.plo : nullptr, P.src, leaf_list,
                                                     split ? 1 : 0, quadrupole ? 1 : 0);
+    long long b2 = ((long long)T.cap / 4 + 255) / 256;
+    if (b2 > 152 * 4) b2 = 152 * 4;
+    if (b2 < 1) b2 = 1;
+    for (int l = kKeyLevels - 1; l >= 0; --l)
+        internal_moments_kernel<<<(unsigned)b2, 256, 0, s>>>(T, C, l, quadrupole ? 1 : 0);
 }
 
 void launch_reset_counters(Counters* C, cudaStream_t s) { reset_counters_kernel<<<1, 32, 0, s>>>(C); }
