@@ -90,6 +90,7 @@ typedef struct ngrav_gpu_ferr {
     double rms;            /* rms of |a - a_ref| / |a_ref| over the sampled targets */
     double max;
     double median;
+    double mean;           /* the --bench error column (main.cpp:323-331) */
     int nsample;
 } ngrav_gpu_ferr;
 

@@ -61,6 +61,7 @@ class Diag(ctypes.Structure):
 
 class Ferr(ctypes.Structure):
     _fields_ = [("rms", ctypes.c_double), ("max", ctypes.c_double), ("median", ctypes.c_double),
+                ("mean", ctypes.c_double),
                 ("nsample", ctypes.c_int)]
 
 
@@ -93,6 +94,24 @@ def library_path() -> str:
     return LIB_PATH
 
 
+EXE_PATH = os.path.join(PKG_DIR, "nbody_gb300")
+
+
+def _run_build():
+    from importlib import util as _u
+    spec = _u.spec_from_file_location("_ngrav_build", os.path.join(PKG_DIR, "build.py"))
+    mod = _u.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+
+
+def executable() -> str:
+    """Path of the deck front end, nbody_gb300 (built with the library if absent)."""
+    if not os.path.isfile(EXE_PATH):
+        _run_build()
+    return EXE_PATH
+
+
 def load_library(path: str | None = None):
     """Load libngrav_gpu.so (building it if absent) and declare the C-ABI."""
     global _lib
@@ -100,11 +119,7 @@ def load_library(path: str | None = None):
         return _lib
     path = path or LIB_PATH
     if not os.path.isfile(path):
-        from importlib import util as _u
-        spec = _u.spec_from_file_location("_ngrav_build", os.path.join(PKG_DIR, "build.py"))
-        mod = _u.module_from_spec(spec)
-        spec.loader.exec_module(mod)
-        mod.build()
+        _run_build()
     L = ctypes.CDLL(path)
     L.ngrav_gpu_default_opts.argtypes = [ctypes.POINTER(Opts)]
     L.ngrav_gpu_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(Opts)]
@@ -276,7 +291,7 @@ class NBodySystem:
         f = Ferr()
         self._check(self.L.ngrav_gpu_force_error(self.h, int(nsample), int(seed), int(fp64_pairs),
                                                  ctypes.byref(f)), self.h)
-        return dict(rms=f.rms, max=f.max, median=f.median, nsample=f.nsample)
+        return dict(rms=f.rms, max=f.max, median=f.median, mean=f.mean, nsample=f.nsample)
 
     def stats(self):
         s = Stats()

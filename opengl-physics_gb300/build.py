@@ -1,9 +1,13 @@
-"""Builds the engine's shared library, libngrav_gpu.so, in-tree.
+"""Builds the engine's shared library, libngrav_gpu.so, and the deck front
+end, nbody_gb300, in-tree.
 
 Every CUDA translation unit under ``csrc/`` is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked into
-``opengl-physics_gb300/libngrav_gpu.so`` next to this file.  Objects go to
-``_build/`` at the repository root.  No cmake; nvcc and the host gcc only.
+``opengl-physics_gb300/libngrav_gpu.so`` next to this file.  The C++ sources
+under ``host/`` (deck parser, output writer, scenarios, CLI) are compiled with
+the host g++ and linked into ``opengl-physics_gb300/nbody_gb300`` against that
+library (rpath ``$ORIGIN``).  Objects go to ``_build/`` at the repository
+root.  No cmake; nvcc and the host gcc only.
 """
 from __future__ import annotations
 
@@ -19,7 +23,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
+HOST = os.path.join(PKG, "host")
 LIB = os.path.join(PKG, "libngrav_gpu.so")
+EXE = os.path.join(PKG, "nbody_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -ftz=true / -prec-sqrt=false: FP32 denormals are flushed and sqrtf is the
@@ -46,6 +52,47 @@ def _deps():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
+HOST_FLAGS = ["-O2", "-std=c++17", "-Wall", "-I", INCLUDE, "-I", HOST]
+
+
+def gxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand and os.path.isfile(cand):
+            return cand
+    raise RuntimeError("g++ not found")
+
+
+def _newer(target: str, deps) -> bool:
+    """True when target exists and is at least as new as every dep."""
+    return os.path.isfile(target) and os.path.getmtime(target) >= max(os.path.getmtime(d) for d in deps)
+
+
+def _compile_host(src: str) -> str:
+    obj = os.path.join(BUILD, "host_" + os.path.basename(src) + ".o")
+    deps = [src] + glob.glob(os.path.join(HOST, "*.hpp")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    if _newer(obj, deps):
+        return obj
+    r = subprocess.run([gxx()] + HOST_FLAGS + ["-c", src, "-o", obj], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
+def build_host(jobs: int | None = None) -> str:
+    """Compile host/*.cpp and link nbody_gb300 against libngrav_gpu.so."""
+    srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
+        objs = list(ex.map(_compile_host, srcs))
+    if not _newer(EXE, objs + [LIB]):
+        tmp = EXE + ".tmp"
+        cmd = [gxx(), "-o", tmp] + objs + ["-L", PKG, "-lngrav_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed for nbody_gb300:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, EXE)
+    return EXE
+
+
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(d) for d in _deps()])
@@ -60,8 +107,9 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     return obj
 
 
-def build(verbose_ptxas: bool = False, jobs: int | None = None) -> str:
-    """Compile and link libngrav_gpu.so; returns its path."""
+def build(verbose_ptxas: bool = False, jobs: int | None = None, host: bool = True) -> str:
+    """Compile and link libngrav_gpu.so (and, with host=True, nbody_gb300);
+    returns the library's path."""
     os.makedirs(BUILD, exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
@@ -74,6 +122,8 @@ def build(verbose_ptxas: bool = False, jobs: int | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    if host:
+        build_host(jobs)
     return LIB
 
 

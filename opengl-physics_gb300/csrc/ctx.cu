@@ -738,6 +738,9 @@ int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp
     out->rms = std::sqrt(s2 / nsample);
     out->max = mx;
     out->median = (nsample & 1) ? rel[nsample / 2] : 0.5 * (rel[nsample / 2 - 1] + rel[nsample / 2]);
+    double sum = 0.0;
+    for (double r : rel) sum += r;
+    out->mean = sum / nsample;
     out->nsample = nsample;
     return NGRAV_OK;
 }

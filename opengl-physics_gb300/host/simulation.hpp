@@ -1,0 +1,92 @@
+// simulation.hpp -- the batch-run contract: fw::Simulation, its static
+// SimInfo, the OutputWriter that records a run, and RunHeadless.
+//
+// Mirrors framework/include/framework/{Simulation,OutputWriter,
+// HeadlessRunner}.hpp of the reference (Simulation.hpp:14-66,
+// OutputWriter.hpp:30-62, HeadlessRunner.hpp:12-20) for the headless path:
+// Configure -> loop { Snapshot; Step } -> manifest.  The interactive/GL hooks
+// (Render, OnViewInput, OnKey) have no counterpart: there is no graphics
+// stack on this system.
+#pragma once
+
+#include <fstream>
+#include <map>
+#include <string>
+#include <string_view>
+#include <vector>
+
+namespace fw {
+
+class Deck;
+class OutputWriter;
+
+struct SimInfo {
+    std::string title;
+    int gridNx = 0;
+    int gridNy = 0;
+    double lx = 0.0;
+    double ly = 0.0;
+    double dt = 0.0;
+    int substepsPerFrame = 1;
+    std::vector<std::string> frameFields;   // .npy fields written per frame
+    std::vector<std::string> diagnostics;   // CSV columns after "t,step"
+};
+
+class Simulation {
+public:
+    virtual ~Simulation() = default;
+    virtual void Configure(const Deck& deck) = 0;
+    virtual void Reset() = 0;
+    virtual void Step(int substeps) = 0;
+    virtual void Snapshot(OutputWriter& writer) = 0;
+    virtual SimInfo Info() const = 0;
+};
+
+// NumPy .npy element types (OutputWriter.hpp:15-17).
+enum class NpyDtype { F4, F8, C8, I4 };
+
+// <dir>/deck.toml, <dir>/manifest.json, <dir>/diagnostics.csv and
+// <dir>/frames/<field>_NNNN.npy, byte-compatible with the reference's writer
+// (framework/src/OutputWriter.cpp:38-167).
+class OutputWriter {
+public:
+    OutputWriter(std::string outDir, const SimInfo& info, const Deck& deck);
+    OutputWriter(const OutputWriter&) = delete;
+    OutputWriter& operator=(const OutputWriter&) = delete;
+
+    void BeginFrame(double t, long step);
+    void WriteField(std::string_view name, const void* data, NpyDtype dtype, int ny, int nx);
+    void WriteScalar(std::string_view name, double value);
+    void EndFrame();
+    void Finish();
+    int FramesWritten() const { return m_frameIndex; }
+
+private:
+    struct FieldMeta {
+        NpyDtype dtype = NpyDtype::F4;
+        int ny = 0;
+        int nx = 0;
+    };
+    std::string m_dir;
+    SimInfo m_info;
+    std::ofstream m_csv;
+    std::map<std::string, FieldMeta> m_fields;
+    std::map<std::string, double> m_pendingScalars;
+    int m_frameIndex = -1;
+    double m_frameT = 0.0;
+    long m_frameStep = 0;
+    bool m_finished = false;
+};
+
+struct HeadlessOptions {
+    std::string outDir;
+    int frames = 0;     // 0 -> deck time.frames (default 200)
+    int substeps = 0;   // 0 -> SimInfo::substepsPerFrame
+    bool quiet = false;
+};
+
+// framework/src/HeadlessRunner.cpp:11-41: write a frame, advance, repeat;
+// then the manifest.  Returns 0.
+int RunHeadless(Simulation& sim, const Deck& deck, const HeadlessOptions& opts);
+
+}  // namespace fw

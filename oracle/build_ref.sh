@@ -20,6 +20,7 @@ mkdir -p "$HERE/_ref"
 g++ -std=gnu++20 -O3 -march=native -funroll-loops -fopenmp -fPIC -shared \
     -I "$HERE/ref_shim" -I "$SRC/include" \
     "$SRC/src/Tree.cpp" "$SRC/src/Solvers.cpp" "$SRC/src/Integrator.cpp" "$SRC/src/MutualFmm.cpp" \
+    "$SRC/src/Scenarios.cpp" \
     "$HERE/ref_driver.cpp" \
     -o "$HERE/_ref/libngrav_ref.so.tmp"
 mv "$HERE/_ref/libngrav_ref.so.tmp" "$HERE/_ref/libngrav_ref.so"

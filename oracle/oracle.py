@@ -253,6 +253,21 @@ class Reference(_Common):
         self.lib.ref_plummer(n, seed, *[_dp(a) for a in arrs])
         return arrs
 
+    def scenario(self, kind, n, seed, ic_file=None):
+        """The reference's deck scenario generator: (x, y, z, vx, vy, vz, m), (G, eps, dt)."""
+        L = self.lib
+        L.ref_scenario.restype = ctypes.c_int
+        L.ref_scenario.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint, ctypes.c_char_p, ctypes.c_int] + \
+            [_D] * 8
+        par = np.zeros(3)
+        icb = ic_file.encode() if ic_file else None
+        count = L.ref_scenario(kind.encode(), n, seed, icb, 0, *([None] * 7), _dp(par))
+        if count < 0:
+            raise RuntimeError(f"reference scenario '{kind}' failed")
+        arrs = [np.zeros(count) for _ in range(7)]
+        L.ref_scenario(kind.encode(), n, seed, icb, count, *[_dp(a) for a in arrs], _dp(par))
+        return arrs, (float(par[0]), float(par[1]), float(par[2]))
+
     def cloud(self, kind, n, seed):
         """Input clouds of the reference self-tests: 'uniform' (BH vs Direct) or 'ball' (quadrupole)."""
         arrs = [np.zeros(n) for _ in range(4)]

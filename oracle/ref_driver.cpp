@@ -14,10 +14,13 @@
 //                          (src/Tree.cpp:33-52,205-254; src/Solvers.cpp:407-415)
 //   ref_tree_*          -> AdaptiveTree<3> node arrays      (include/ngrav/Tree.hpp:44-63)
 //   ref_leapfrog        -> ngrav::LeapfrogStep<3>           (src/Integrator.cpp:9-39)
+//   ref_scenario        -> ngrav::BuildScenario<3>(ScenarioFromString(type), params)
+//                          (src/Scenarios.cpp:355-384)
 //   ref_diagnostics     -> System<3>::TotalEnergy / CenterOfMass / AngularMomentum
 //                          (include/ngrav/System.hpp:119-193) and the momentum sum of
 //                          DeckSim::Snapshot (src/DeckSim.cpp:147-153)
 #include "ngrav/Integrator.hpp"
+#include "ngrav/Scenarios.hpp"
 #include "ngrav/Solvers.hpp"
 #include "ngrav/System.hpp"
 #include "ngrav/Tree.hpp"
@@ -286,6 +289,38 @@ void ref_diagnostics(int n, const double* x, const double* y, const double* z, c
     out[7] = px;
     out[8] = py;
     out[9] = pz;
+}
+
+// The deck scenario generator.  Call with cap = 0 to learn the particle count
+// (returned); then with cap >= count to receive the arrays.  params[0..2] =
+// G, softening eps, suggested dt.  Returns -1 on an exception.
+int ref_scenario(const char* type, int n, unsigned seed, const char* ic_file, int cap, double* x, double* y,
+                 double* z, double* vx, double* vy, double* vz, double* m, double* params) {
+    try {
+        ScenarioParams pp;
+        pp.n = n;
+        pp.seed = seed;
+        pp.icFile = ic_file ? ic_file : "";
+        const Scenario<3> sc = BuildScenario<3>(ScenarioFromString(type, ScenarioType::PlummerSphere), pp);
+        const int count = static_cast<int>(sc.state.x.size());
+        if (cap >= count) {
+            for (int i = 0; i < count; ++i) {
+                x[i] = sc.state.x[i];
+                y[i] = sc.state.y[i];
+                z[i] = sc.state.z[i];
+                vx[i] = sc.state.vx[i];
+                vy[i] = sc.state.vy[i];
+                vz[i] = sc.state.vz[i];
+                m[i] = sc.state.m[i];
+            }
+        }
+        params[0] = sc.G;
+        params[1] = sc.soft.eps;
+        params[2] = sc.suggestedDt;
+        return count;
+    } catch (...) {
+        return -1;
+    }
 }
 
 } // extern "C"

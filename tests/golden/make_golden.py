@@ -9,7 +9,8 @@ writes are committed so that tests never need the reference at run time.
 All positions and masses are rounded to FP32 before the reference sees them,
 so the GPU state (FP32 / double-float) holds exactly the same inputs.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # every fixture
+    python tests/golden/make_golden.py scenarios    # scenarios.npz only
 """
 from __future__ import annotations
 
@@ -38,11 +39,36 @@ def tree_fields(R, x, y, z, m, ncrit, tag):
     return out
 
 
+# Deck scenarios (Scenarios.cpp:355-384) as the reference generates them,
+# stored as the raw 7 x float32 records its ic_file / --dump-ic format holds
+# (x, y, z, m, vx, vy, vz), plus the scenario's G, softening and dt.
+SCENARIOS = (("plummer", 3000, 5), ("cluster", 2500, 2), ("cold_collapse", 5000, 1), ("plummer_sphere", 100, 9))
+
+
+def make_scenarios(R):
+    d = {}
+    for kind, n, seed in SCENARIOS:
+        (x, y, z, vx, vy, vz, m), par = R.scenario(kind, n, seed)
+        d[f"{kind}_rec"] = np.stack([x, y, z, m, vx, vy, vz], 1).astype(np.float32)
+        d[f"{kind}_params"] = np.array(par)
+        d[f"{kind}_n"] = n
+        d[f"{kind}_seed"] = seed
+    # The --bench / --dump-ic Plummer sphere (main.cpp:243-280): seed 1.
+    for n in (1000, 4097):
+        x, y, z, vx, vy, vz, m = R.plummer(n, 1)
+        d[f"bench{n}_rec"] = np.stack([x, y, z, m, vx, vy, vz], 1).astype(np.float32)
+    d["names"] = np.array([k for k, _, _ in SCENARIOS])
+    np.savez_compressed(os.path.join(HERE, "scenarios.npz"), **d)
+
+
 def main():
     orc = ge.load_oracle()
     if orc.build_reference() is None:
         raise SystemExit("reference sources not found; set NGRAV_REFERENCE")
     R = orc.Reference()
+    make_scenarios(R)
+    if sys.argv[1:] == ["scenarios"]:
+        return
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
 
     # 1) Plummer N=16,384, seed 0: leaf capacity 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK steps.
