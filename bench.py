@@ -49,6 +49,11 @@ WORKLOADS = {
     "plummer1m": ("plummer", {"n": 1048576, "seed": 1}, 0.005, 5e-4, 0.5, 16),
     "plummer16k": ("plummer", {"n": 16384, "seed": 0}, 0.01, 1e-3, 0.5, 16),
 }
+# DRAM bytes (read + write) per interaction-list entry of one eval_kernel launch,
+# from dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture at
+# N = 1,048,576 (1.350 GB for 3.32e8 entries; profiles/eval_kernel_galaxy1m.txt).
+# The lists are the kernel's only DRAM stream, so traffic scales with entries.
+EVAL_DRAM_BYTES_PER_LIST_ENTRY = 4.07
 METRIC = "particle-steps/s at N=4M, learned-MAC vs plain θ-MAC at equal 1e-3 rms force err"
 
 
@@ -282,7 +287,9 @@ def main():
                                                                   "ms_moments", "ms_walk", "ms_force")},
                        "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"])},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                         "frac": (achieved / peak) if achieved and peak else None,
+                         "traffic": EVAL_DRAM_BYTES_PER_LIST_ENTRY * (st["far_entries"] + st["near_entries"]),
+                         "traffic_unit": "DRAM bytes per eval_kernel launch (ncu bytes/entry x entries)",
                          "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
                          "peak_source": "measured FP32 FMA probe (ngrav_gpu_probe_fp32_peak)"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,

@@ -121,6 +121,13 @@ typedef struct ngrav_gpu_stats {
     /* interaction lists of the last evaluation */
     long long far_entries, near_entries;
     int list_max;          /* longest per-group list */
+    /* learned opening test, last evaluation: pairs handed to the network,
+     * accepted by it, decided by the geometric fallback (low confidence);
+     * tensor-core flushes; whether it ran, whether the run reverted to the
+     * geometric test, checks made and the last checked rms error */
+    long long lmac_queries, lmac_accepts, lmac_fallbacks, lmac_flushes;
+    int lmac_active, lmac_reverted, lmac_checks;
+    double lmac_last_check_rms;
 } ngrav_gpu_stats;
 
 typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;
@@ -218,6 +225,79 @@ int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const f
  *   count          particles under each node; is_leaf
  *   center[3*nn], half, com[3*nn], mass, max_radius, quad[5*nn] (Qxx Qyy Qxy Qxz Qyz)
  * Node numbering is the GPU's own; compare in (level, prefix) order. */
+/* ---- learned opening test (NGRAV_MAC_LEARNED) --------------------------
+ * No reference counterpart: it replaces the geometric test of
+ * include/ngrav/Mac.hpp:25-29 / src/Solvers.cpp:261-271 inside the grouped
+ * walk.  A network of 8 features -> 32 -> 32 -> 1 predicts whether a node's
+ * multipole keeps every member of the target group within the per-target
+ * error budget; it is trained on the GPU (ngrav_gpu_lmac_train) on pairs
+ * the method labels itself, evaluated in BF16 on the tensor cores inside the
+ * walk, backed by the geometric test where it is not confident, and checked
+ * every check_every evaluations against the FP64 direct sum on
+ * check_targets samples: above revert_rms the run reverts to the geometric
+ * test for good. */
+#define NGRAV_LMAC_PARAMS 1377  /* W1[32][8], b1[32], W2[32][32], b2[32], w3[32], b3 */
+#define NGRAV_LMAC_FEATURES 8
+
+typedef struct ngrav_gpu_lmac_opts {
+    double budget;         /* per-target error budget of one accepted node */
+    double gate;           /* |logit| below which the geometric test decides */
+    double rho_lo, rho_hi; /* 2h/worst at or below rho_lo: accept; at or above rho_hi: open */
+    int check_every;       /* evaluations between FP64 checks (0: never) */
+    int check_targets;     /* sampled targets of one check */
+    double revert_rms;     /* rms relative force error that triggers the revert */
+} ngrav_gpu_lmac_opts;
+
+typedef struct ngrav_gpu_lmac_train_opts {
+    int snapshots;         /* states the training pairs are drawn from */
+    int steps_between;     /* KDK steps (geometric test) between snapshots */
+    double dt;             /* their step; 0 keeps the state fixed */
+    long long pairs;       /* labelled (group, node) pairs in total */
+    double theta_record;   /* geometric test of the recording walk */
+    double u_range;        /* budgets drawn at r * 2^U(-u_range, u_range) */
+    int epochs;            /* passes over the training pairs */
+    int batch;             /* mini-batch size (multiple of 128) */
+    double lr;             /* Adam step size */
+    uint64_t seed;
+} ngrav_gpu_lmac_train_opts;
+
+typedef struct ngrav_gpu_lmac_report {
+    long long pairs;       /* labelled pairs kept (training + held out) */
+    long long band_pairs;  /* band pairs the recording walks met */
+    double loss_first, loss_last, acc_last;  /* training BCE and accuracy */
+    double val_loss, val_acc;                /* held-out pairs */
+    double ms_data, ms_train;
+} ngrav_gpu_lmac_report;
+
+int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o);
+int ngrav_gpu_lmac_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_lmac_opts* o);
+int ngrav_gpu_lmac_default_train_opts(ngrav_gpu_lmac_train_opts* o);
+/* Generate pairs on the current system (advancing it between snapshots with
+ * the geometric test), train from a fresh initialisation and install the
+ * model.  The system's state afterwards is the last snapshot's. */
+int ngrav_gpu_lmac_train(ngrav_gpu_ctx* ctx, const ngrav_gpu_lmac_train_opts* o, ngrav_gpu_lmac_report* out);
+/* FP32 parameters (NGRAV_LMAC_PARAMS) and the feature standardisation
+ * (mu[8], 1/sd[8]). */
+int ngrav_gpu_lmac_get_model(ngrav_gpu_ctx* ctx, float* params, float* norm);
+int ngrav_gpu_lmac_set_model(ngrav_gpu_ctx* ctx, const float* params, const float* norm);
+/* Clear the revert flag (the next learned evaluation uses the network again). */
+int ngrav_gpu_lmac_reset(ngrav_gpu_ctx* ctx);
+/* Inspection: pairs of the current tree met in the band by a recording walk
+ * at theta_record, each kept with probability keep; their group leaf and node
+ * ids (numbering of ngrav_gpu_debug_tree), unit-budget features and measured
+ * worst relative multipole error r (-1: group too large to label). */
+int ngrav_gpu_lmac_collect(ngrav_gpu_ctx* ctx, double theta_record, double rho_lo, double rho_hi, double keep,
+                           uint64_t seed, int cap, int* npairs, long long* nband, int* group_leaf, int* node,
+                           float* features, float* r);
+/* Network outputs: FP32 on standardised features (the training forward
+ * pass), or BF16 on the tensor cores from raw features (the walk's path). */
+int ngrav_gpu_lmac_forward(ngrav_gpu_ctx* ctx, const float* x_std, int n, float* z);
+int ngrav_gpu_lmac_forward_tc(ngrav_gpu_ctx* ctx, const float* x_raw, int n, float* z);
+/* Gradient of scale * sum_k w_k BCE(z_k, y_k) at `params` (NULL: the
+ * installed model) on standardised features; loss = sum_k w_k BCE. */
+int ngrav_gpu_lmac_grad(ngrav_gpu_ctx* ctx, const float* x_std, const float* y, const float* w, int n,
+                        const float* params, double scale, float* grad, double* loss);
+
 int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* order, int* level, uint64_t* prefix,
                          int* count, int* is_leaf, double* center, double* half, double* com, double* mass,
                          double* max_radius, double* quad);

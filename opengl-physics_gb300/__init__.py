@@ -41,7 +41,12 @@ EXPORTS = (
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
+    "ngrav_gpu_lmac_default_opts", "ngrav_gpu_lmac_set_opts", "ngrav_gpu_lmac_default_train_opts",
+    "ngrav_gpu_lmac_train", "ngrav_gpu_lmac_get_model", "ngrav_gpu_lmac_set_model", "ngrav_gpu_lmac_reset",
+    "ngrav_gpu_lmac_collect", "ngrav_gpu_lmac_forward", "ngrav_gpu_lmac_forward_tc", "ngrav_gpu_lmac_grad",
 )
+LMAC_PARAMS = 1377
+LMAC_FEATURES = 8
 NOALLOC_MAX_N = 16777216
 
 
@@ -77,7 +82,32 @@ class Stats(ctypes.Structure):
                 ("cum_p2c_terms", ctypes.c_longlong), ("cum_ms_walk", ctypes.c_double),
                 ("cum_ms_force", ctypes.c_double), ("cum_ms_eval", ctypes.c_double),
                 ("cum_ms_step", ctypes.c_double), ("cum_launches", ctypes.c_longlong),
-                ("far_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong), ("list_max", ctypes.c_int)]
+                ("far_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong), ("list_max", ctypes.c_int),
+                ("lmac_queries", ctypes.c_longlong), ("lmac_accepts", ctypes.c_longlong),
+                ("lmac_fallbacks", ctypes.c_longlong), ("lmac_flushes", ctypes.c_longlong),
+                ("lmac_active", ctypes.c_int), ("lmac_reverted", ctypes.c_int), ("lmac_checks", ctypes.c_int),
+                ("lmac_last_check_rms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LmacOpts(ctypes.Structure):
+    _fields_ = [("budget", ctypes.c_double), ("gate", ctypes.c_double), ("rho_lo", ctypes.c_double),
+                ("rho_hi", ctypes.c_double), ("check_every", ctypes.c_int), ("check_targets", ctypes.c_int),
+                ("revert_rms", ctypes.c_double)]
+
+
+class LmacTrainOpts(ctypes.Structure):
+    _fields_ = [("snapshots", ctypes.c_int), ("steps_between", ctypes.c_int), ("dt", ctypes.c_double),
+                ("pairs", ctypes.c_longlong), ("theta_record", ctypes.c_double), ("u_range", ctypes.c_double),
+                ("epochs", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+class LmacReport(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_longlong), ("band_pairs", ctypes.c_longlong), ("loss_first", ctypes.c_double),
+                ("loss_last", ctypes.c_double), ("acc_last", ctypes.c_double), ("val_loss", ctypes.c_double),
+                ("val_acc", ctypes.c_double), ("ms_data", ctypes.c_double), ("ms_train", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -144,6 +174,20 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_probe_fp32_peak.argtypes = [ctypes.c_int, _D]
     L.ngrav_gpu_diagnostics_noalloc.argtypes = [ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 7 + \
         [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Diag)]
+    L.ngrav_gpu_lmac_default_opts.argtypes = [ctypes.POINTER(LmacOpts)]
+    L.ngrav_gpu_lmac_set_opts.argtypes = [ctypes.c_void_p, ctypes.POINTER(LmacOpts)]
+    L.ngrav_gpu_lmac_default_train_opts.argtypes = [ctypes.POINTER(LmacTrainOpts)]
+    L.ngrav_gpu_lmac_train.argtypes = [ctypes.c_void_p, ctypes.POINTER(LmacTrainOpts), ctypes.POINTER(LmacReport)]
+    L.ngrav_gpu_lmac_get_model.argtypes = [ctypes.c_void_p, _F, _F]
+    L.ngrav_gpu_lmac_set_model.argtypes = [ctypes.c_void_p, _F, _F]
+    L.ngrav_gpu_lmac_reset.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_lmac_collect.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_uint64, ctypes.c_int, _I,
+                                         ctypes.POINTER(ctypes.c_longlong), _I, _I, _F, _F]
+    L.ngrav_gpu_lmac_forward.argtypes = [ctypes.c_void_p, _F, ctypes.c_int, _F]
+    L.ngrav_gpu_lmac_forward_tc.argtypes = [ctypes.c_void_p, _F, ctypes.c_int, _F]
+    L.ngrav_gpu_lmac_grad.argtypes = [ctypes.c_void_p, _F, _F, _F, ctypes.c_int, _F, ctypes.c_double, _F,
+                                      ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -315,6 +359,78 @@ class NBodySystem:
             _p(t["half"], _D), _p(t["com"], _D), _p(t["mass"], _D), _p(t["max_radius"], _D),
             _p(t["quad"], _D)), self.h)
         return t
+
+
+    # ---- learned opening test ----
+    def lmac_set_opts(self, **kw):
+        """Run-time options of the learned test (budget, gate, rho_lo/rho_hi, check_every,
+        check_targets, revert_rms); unspecified ones keep the library defaults."""
+        o = LmacOpts()
+        self._check(self.L.ngrav_gpu_lmac_default_opts(ctypes.byref(o)), None)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        self._check(self.L.ngrav_gpu_lmac_set_opts(self.h, ctypes.byref(o)), self.h)
+
+    def lmac_train(self, **kw):
+        """Generate labelled pairs on this system and train the network; returns the report."""
+        o = LmacTrainOpts()
+        self._check(self.L.ngrav_gpu_lmac_default_train_opts(ctypes.byref(o)), None)
+        for k, v in kw.items():
+            setattr(o, k, v)
+        r = LmacReport()
+        self._check(self.L.ngrav_gpu_lmac_train(self.h, ctypes.byref(o), ctypes.byref(r)), self.h)
+        return r.as_dict()
+
+    def lmac_get_model(self):
+        p = np.zeros(LMAC_PARAMS, np.float32)
+        nrm = np.zeros(2 * LMAC_FEATURES, np.float32)
+        self._check(self.L.ngrav_gpu_lmac_get_model(self.h, _p(p, _F), _p(nrm, _F)), self.h)
+        return p, nrm
+
+    def lmac_set_model(self, params, norm):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        nrm = np.ascontiguousarray(norm, dtype=np.float32)
+        self._check(self.L.ngrav_gpu_lmac_set_model(self.h, _p(p, _F), _p(nrm, _F)), self.h)
+
+    def lmac_reset(self):
+        self._check(self.L.ngrav_gpu_lmac_reset(self.h), self.h)
+
+    def lmac_collect(self, theta_record=0.3, rho_lo=0.25, rho_hi=1.25, keep=1.0, seed=1, cap=65536):
+        """Band pairs of the current tree with their features and labels."""
+        npairs = ctypes.c_int()
+        nband = ctypes.c_longlong()
+        g = np.zeros(cap, np.int32)
+        nd = np.zeros(cap, np.int32)
+        X = np.zeros((cap, LMAC_FEATURES), np.float32)
+        r = np.zeros(cap, np.float32)
+        self._check(self.L.ngrav_gpu_lmac_collect(self.h, theta_record, rho_lo, rho_hi, keep, int(seed), int(cap),
+                                                  ctypes.byref(npairs), ctypes.byref(nband), _p(g, _I), _p(nd, _I),
+                                                  _p(X, _F), _p(r, _F)), self.h)
+        k = npairs.value
+        return dict(group=g[:k], node=nd[:k], X=X[:k], r=r[:k], nband=nband.value)
+
+    def lmac_forward(self, x_std):
+        x = np.ascontiguousarray(x_std, dtype=np.float32)
+        z = np.zeros(len(x), np.float32)
+        self._check(self.L.ngrav_gpu_lmac_forward(self.h, _p(x, _F), len(x), _p(z, _F)), self.h)
+        return z
+
+    def lmac_forward_tc(self, x_raw):
+        x = np.ascontiguousarray(x_raw, dtype=np.float32)
+        z = np.zeros(len(x), np.float32)
+        self._check(self.L.ngrav_gpu_lmac_forward_tc(self.h, _p(x, _F), len(x), _p(z, _F)), self.h)
+        return z
+
+    def lmac_grad(self, x_std, y, w=None, params=None, scale=1.0):
+        x = np.ascontiguousarray(x_std, dtype=np.float32)
+        yy = np.ascontiguousarray(y, dtype=np.float32)
+        ww = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        pp = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        g = np.zeros(LMAC_PARAMS, np.float32)
+        loss = ctypes.c_double()
+        self._check(self.L.ngrav_gpu_lmac_grad(self.h, _p(x, _F), _p(yy, _F), _p(ww, _F), len(x), _p(pp, _F),
+                                               float(scale), _p(g, _F), ctypes.byref(loss)), self.h)
+        return g, loss.value
 
 
 def canonical(tree: dict) -> dict:

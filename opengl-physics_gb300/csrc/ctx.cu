@@ -12,6 +12,7 @@
 // re-runs the evaluation.
 #include "ngrav_gpu.h"
 
+#include "ctx_internal.cuh"
 #include "ctx_kernels.cuh"
 #include "engine.cuh"
 
@@ -25,70 +26,7 @@
 #include <vector>
 
 using namespace ngrav;
-
-struct ngrav_gpu_ctx {
-    ngrav_gpu_opts opts{};
-    std::string err;
-    cudaStream_t stream = nullptr;
-    int sm_count = 0;
-    long long n = 0;
-    long long cap_n = 0;
-    Particles P;
-    SortBuffers SB;
-    NodeArrays T;
-    Counters* C = nullptr;
-    Counters hc{};
-    int* leaf_at = nullptr;
-    unsigned* flags = nullptr;
-    unsigned* scanbuf = nullptr;
-    int* leaf_list = nullptr;
-    ListBuffers LB;
-    int eval_nwarps = 0;
-    long long gi_cap = 0;
-    bool walk_global_stack = false;
-    double* stage = nullptr;          // 7 * cap_n doubles (upload / download staging)
-    double* dpartial = nullptr;
-    long long dpartial_cap = 0;
-    int* inv = nullptr;
-    int* dtargets = nullptr;
-    int* dslots = nullptr;
-    double* dsamp = nullptr;
-    int samp_cap = 0;
-    bool have = false;
-    bool primed = false;
-    long long force_evals = 0;
-    cudaEvent_t ev[8] = {};
-    cudaEvent_t sev[2] = {};
-    bool events = false;
-    double phase_ms[7] = {};
-    // cumulative measurement counters (ngrav_gpu_reset_cumulative)
-    long long launches = 0;
-    long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
-    double cum_ms_walk = 0.0, cum_ms_force = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
-};
-
-namespace {
-
-#define NG_CUDA(call)                                                                      \
-    do {                                                                                   \
-        cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess) {                                                           \
-            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
-            return (e_ == cudaErrorMemoryAllocation) ? NGRAV_ERR_OOM : NGRAV_ERR_CUDA;     \
-        }                                                                                  \
-    } while (0)
-
-#define NG_TRY(expr)          \
-    do {                      \
-        int rc_ = (expr);     \
-        if (rc_) return rc_;  \
-    } while (0)
-
-template <typename T>
-void dfree(T*& p) {
-    if (p) cudaFree((void*)p);
-    p = nullptr;
-}
+namespace ngrav_ctx {
 
 int fail(ngrav_gpu_ctx* ctx, int code, const std::string& msg) {
     ctx->err = msg;
@@ -129,14 +67,9 @@ void free_nodes(ngrav_gpu_ctx* ctx) {
     NodeArrays& T = ctx->T;
     dfree(T.start); dfree(T.count); dfree(T.first_child); dfree(T.parent); dfree(T.visit);
     dfree(T.nchild); dfree(T.level); dfree(T.cx); dfree(T.cy); dfree(T.cz);
-    dfree(T.mass); dfree(T.comx); dfree(T.comy); dfree(T.comz); dfree(T.maxr); dfree(T.quad);
+    dfree(T.mass); dfree(T.comx); dfree(T.comy); dfree(T.comz); dfree(T.maxr); dfree(T.quad); dfree(T.amin);
     dfree(T.wA); dfree(T.wB); dfree(T.wC); dfree(T.wD); dfree(T.chi); dfree(T.clo);
     T.cap = 0;
-}
-
-template <typename T>
-cudaError_t dalloc(T*& p, long long count) {
-    return cudaMalloc((void**)&p, sizeof(T) * (size_t)(count > 0 ? count : 1));
 }
 
 int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
@@ -173,6 +106,7 @@ int alloc_nodes(ngrav_gpu_ctx* ctx, int cap) {
     NG_CUDA(dalloc(T.level, cap)); NG_CUDA(dalloc(T.cx, cap)); NG_CUDA(dalloc(T.cy, cap)); NG_CUDA(dalloc(T.cz, cap));
     NG_CUDA(dalloc(T.mass, cap)); NG_CUDA(dalloc(T.comx, cap)); NG_CUDA(dalloc(T.comy, cap));
     NG_CUDA(dalloc(T.comz, cap)); NG_CUDA(dalloc(T.maxr, cap)); NG_CUDA(dalloc(T.quad, 5LL * cap));
+    NG_CUDA(dalloc(T.amin, cap));
     NG_CUDA(dalloc(T.wA, cap)); NG_CUDA(dalloc(T.wB, cap)); NG_CUDA(dalloc(T.wC, cap)); NG_CUDA(dalloc(T.wD, cap));
     NG_CUDA(dalloc(T.chi, cap)); NG_CUDA(dalloc(T.clo, cap));
     T.cap = cap;
@@ -280,8 +214,12 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     launch_moments(ctx->T, ctx->C, P, ctx->leaf_list, n, (int)std::min<long long>(n, ctx->T.cap), split,
                    ctx->opts.quadrupole != 0, s);
     rec(ctx, 4);
-    const WalkParams wp = walk_params(ctx, kick, hdt);
-    launch_walk(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, s);
+    WalkParams wp = walk_params(ctx, kick, hdt);
+    const void* model = nullptr;
+    if (lmac_walk_setup(ctx, wp, &model))
+        lmac_launch_walk(ctx, wp, model);
+    else
+        launch_walk(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, s);
     rec(ctx, 5);
     launch_eval(ctx->T, ctx->C, P, ctx->leaf_list, wp, ctx->LB, ctx->eval_nwarps, s);
     rec(ctx, 6);
@@ -345,6 +283,7 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
                             ctx->phase_ms[4] + ctx->phase_ms[5];
     }
     ctx->force_evals += 1;
+    ctx->acc_valid = true;
     ctx->cum_evals += 1;
     ctx->cum_pairs += (long long)ctx->hc.p2p_pairs;
     ctx->cum_p2c += (long long)ctx->hc.p2c_terms;
@@ -357,7 +296,7 @@ int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
         enqueue_eval(ctx, bbox_ready, kick, hdt);
         bool retry = false;
         NG_TRY(finish_eval(ctx, retry));
-        if (!retry) return NGRAV_OK;
+        if (!retry) return lmac_after_eval(ctx);
         bbox_ready = false;
     }
     return fail(ctx, NGRAV_ERR_CAPACITY, "capacity growth did not converge");
@@ -426,10 +365,13 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
     }
     ctx->have = n > 0;
     ctx->primed = false;
+    ctx->acc_valid = false;
     return NGRAV_OK;
 }
 
-}  // namespace
+}  // namespace ngrav_ctx
+
+using namespace ngrav_ctx;
 
 extern "C" {
 
@@ -495,6 +437,7 @@ void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->opts.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    lmac_destroy(ctx);
     free_particles(ctx);
     free_nodes(ctx);
     dfree(ctx->C);
@@ -782,6 +725,7 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->cum_ms_eval = ctx->cum_ms_eval;
     out->cum_ms_step = ctx->cum_ms_step;
     out->cum_launches = ctx->launches;
+    lmac_fill_stats(ctx, out);
     return NGRAV_OK;
 }
 

@@ -1,0 +1,106 @@
+// ctx_internal.cuh -- the context behind the C-ABI handle and the host
+// helpers shared by the translation units that implement include/ngrav_gpu.h
+// (ctx.cu: state, force evaluation, KDK; lmac_host.cu: the learned opening
+// test).
+#pragma once
+
+#include "ngrav_gpu.h"
+
+#include "engine.cuh"
+
+#include <string>
+
+using namespace ngrav;
+
+namespace ngrav_ctx {
+struct LmacState;  // lmac_host.cu
+}
+
+struct ngrav_gpu_ctx {
+    ngrav_gpu_opts opts{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    long long n = 0;
+    long long cap_n = 0;
+    Particles P;
+    SortBuffers SB;
+    NodeArrays T;
+    Counters* C = nullptr;
+    Counters hc{};
+    int* leaf_at = nullptr;
+    unsigned* flags = nullptr;
+    unsigned* scanbuf = nullptr;
+    int* leaf_list = nullptr;
+    ListBuffers LB;
+    int eval_nwarps = 0;
+    long long gi_cap = 0;
+    bool walk_global_stack = false;
+    double* stage = nullptr;          // 7 * cap_n doubles (upload / download staging)
+    double* dpartial = nullptr;
+    long long dpartial_cap = 0;
+    int* inv = nullptr;
+    int* dtargets = nullptr;
+    int* dslots = nullptr;
+    double* dsamp = nullptr;
+    int samp_cap = 0;
+    bool have = false;
+    bool primed = false;
+    long long force_evals = 0;
+    cudaEvent_t ev[8] = {};
+    cudaEvent_t sev[2] = {};
+    bool events = false;
+    double phase_ms[7] = {};
+    // cumulative measurement counters (ngrav_gpu_reset_cumulative)
+    long long launches = 0;
+    long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
+    double cum_ms_walk = 0.0, cum_ms_force = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
+    bool acc_valid = false;           // P.acc holds a force evaluation of this particle set
+    // learned opening test (model, training buffers, run-time control)
+    ngrav_ctx::LmacState* lm = nullptr;
+};
+
+namespace ngrav_ctx {
+
+#define NG_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+            return (e_ == cudaErrorMemoryAllocation) ? NGRAV_ERR_OOM : NGRAV_ERR_CUDA;     \
+        }                                                                                  \
+    } while (0)
+
+#define NG_TRY(expr)          \
+    do {                      \
+        int rc_ = (expr);     \
+        if (rc_) return rc_;  \
+    } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+template <typename T>
+cudaError_t dalloc(T*& p, long long count) {
+    return cudaMalloc((void**)&p, sizeof(T) * (size_t)(count > 0 ? count : 1));
+}
+
+int fail(ngrav_gpu_ctx* ctx, int code, const std::string& msg);
+bool split_of(const ngrav_gpu_ctx* ctx);
+ngrav::WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt);
+// One force evaluation of the current state (retrying on capacity growth).
+int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt);
+
+// Learned opening test hooks (lmac_host.cu).
+void lmac_destroy(ngrav_gpu_ctx* ctx);
+// True when the next walk uses the learned test; fills the walk parameters.
+bool lmac_walk_setup(ngrav_gpu_ctx* ctx, ngrav::WalkParams& wp, const void** model);
+void lmac_launch_walk(ngrav_gpu_ctx* ctx, const ngrav::WalkParams& wp, const void* model);
+// After a force evaluation: run the periodic FP64 check, revert on a breach.
+int lmac_after_eval(ngrav_gpu_ctx* ctx);
+void lmac_fill_stats(const ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out);
+
+}  // namespace ngrav_ctx

@@ -64,6 +64,12 @@ struct Counters {
     int far_chunks;                   // chunk allocators (may exceed the pool: then
     int near_chunks;                  //   they count what a retry needs)
     int pad2;
+    // learned opening test: pairs handed to the network, accepted by it, and
+    // decided by the geometric fallback (low confidence); tensor-core flushes
+    unsigned long long lm_queries;
+    unsigned long long lm_accepts;
+    unsigned long long lm_fallbacks;
+    unsigned long long lm_flushes;
 };
 
 // Per-group interaction lists written by the walk, read by the evaluation.
@@ -101,6 +107,7 @@ struct NodeArrays {
     double* comz = nullptr;
     double* maxr = nullptr;
     double* quad = nullptr;           // 5 per node
+    float* amin = nullptr;            // leaves: min |a| over the members (learned opening test)
     // FP32 walk records
     float4* wA = nullptr;             // com_hi.xyz, mass
     float4* wB = nullptr;             // Qxx, Qyy, Qxy, Qxz
@@ -159,6 +166,11 @@ struct WalkParams {
     int stack_cap;
     int node_limit;                   // visits per group beyond this mean a corrupt tree
     int global_stack;                 // walk stack in global memory (fallback for deep frontiers)
+    // learned opening test (walk_lmac_kernel)
+    int learned;
+    float lm_log2b;                   // log2 of the per-target error budget
+    float lm_gate;                    // |logit| below which the geometric test decides
+    float lm_rho_lo, lm_rho_hi;       // band of 2h/worst handed to the network
 };
 
 // ---- launchers (each enqueues on `s`; no host synchronisation) ----

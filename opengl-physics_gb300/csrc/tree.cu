@@ -208,8 +208,12 @@ __device__ __forceinline__ void write_walk_record(NodeArrays& T, int node, doubl
                              (float)Q[4]);
 }
 
+// Leaf moments, plus the group acceleration scale amin[leaf] = min over the
+// members of |a| from `acc` (the accelerations carried into this tree order;
+// zero before the first evaluation) that the learned opening test reads.
 __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C, const float4* __restrict__ pos,
                                                       const float4* __restrict__ plo, float4* __restrict__ src,
+                                                      const float4* __restrict__ acc,
                                                       const int* __restrict__ leaf_list, int split, int quadrupole) {
     const int nleaves = C->nleaves;
     const double root_half = C->root_half;
@@ -242,9 +246,12 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         }
         double maxr2 = 0.0;
         float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f, q4 = 0.f;
+        float amin2 = 3.0e38f;
         const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int j = s; j < s + cnt; ++j) {
             const float4 p = pos[j];
+            const float4 a = acc[j];
+            amin2 = fminf(amin2, a.x * a.x + a.y * a.y + a.z * a.z);
             const float4 l = plo ? plo[j] : zero4;
             const double x = (double)p.x + (double)l.x, y = (double)p.y + (double)l.y, z = (double)p.z + (double)l.z;
             const double dx = x - cx, dy = y - cy, dz = z - cz;
@@ -270,6 +277,7 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         T.comy[leaf] = cy;
         T.comz[leaf] = cz;
         T.maxr[leaf] = maxr;
+        T.amin[leaf] = cnt > 0 ? sqrtf(amin2) : 0.f;
         for (int k = 0; k < 5; ++k) T.quad[5 * leaf + k] = Q[k];
         const int level = T.level[leaf];
         write_walk_record(T, leaf, M, cx, cy, cz, Q, maxr, true, s, cnt, level, root_half);
@@ -281,8 +289,10 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
 
 // Internal nodes of one level, from their (finished) children, in FP64: mass,
 // COM (sum m x / M), traceless quadrupole by the parallel-axis shift
-// (Tree.cpp:235-251).  maxRadius of internal nodes is not needed by the
-// walk (only leaves are groups); the tree export derives it on the host.
+// (Tree.cpp:235-251) and maxRadius = max over children of
+// maxR_c + |com_c - com| (Tree.cpp:194-201; massless nodes keep 0).  The
+// geometric opening test reads maxRadius of leaves only; the learned one reads
+// it for every node.
 __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, const Counters* __restrict__ C, int l,
                                                               int quadrupole) {
     const int begin = C->level_begin[l];
@@ -321,12 +331,20 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
                 PQ[4] += T.quad[5 * c + 4] + mc * 3.0 * dy * dz;
             }
         }
+        double mr = 0.0;
+        if (PM > 0.0) {
+            for (int c = fc; c < fc + nch; ++c) {
+                const double dx = T.comx[c] - pcx, dy = T.comy[c] - pcy, dz = T.comz[c] - pcz;
+                mr = fmax(mr, T.maxr[c] + sqrt(dx * dx + dy * dy + dz * dz));
+            }
+        }
         T.mass[node] = PM;
         T.comx[node] = pcx;
         T.comy[node] = pcy;
         T.comz[node] = pcz;
+        T.maxr[node] = mr;
         for (int k = 0; k < 5; ++k) T.quad[5 * node + k] = PQ[k];
-        write_walk_record(T, node, PM, pcx, pcy, pcz, PQ, 0.0, false, fc, nch, l, root_half);
+        write_walk_record(T, node, PM, pcx, pcy, pcz, PQ, mr, false, fc, nch, l, root_half);
     }
 }
 
@@ -335,7 +353,7 @@ void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* l
     long long blocks = ((long long)max_leaves + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
-    moments_kernel<<<(unsigned)blocks, 128, 0, s>>>(T, C, P.pos, split ? P.plo : nullptr, P.src, leaf_list,
+    moments_kernel<<<(unsigned)blocks, 128, 0, s>>>(T, C, P.pos, split ? P.plo : nullptr, P.src, P.acc, leaf_list,
                                                     split ? 1 : 0, quadrupole ? 1 : 0);
     long long b2 = ((long long)T.cap / 4 + 255) / 256;
     if (b2 > 152 * 4) b2 = 152 * 4;

@@ -45,12 +45,27 @@ def test_struct_layouts_match_header(pkg, tmp_path):
     src = tmp_path / "sizes.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "ngrav_gpu.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(ngrav_gpu_opts), sizeof(ngrav_gpu_diag),"
-        " sizeof(ngrav_gpu_ferr), sizeof(ngrav_gpu_stats), offsetof(ngrav_gpu_opts, G),"
-        " offsetof(ngrav_gpu_stats, p2p_pairs));return 0;}\n")
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(ngrav_gpu_opts),"
+        " sizeof(ngrav_gpu_diag), sizeof(ngrav_gpu_ferr), sizeof(ngrav_gpu_stats), offsetof(ngrav_gpu_opts, G),"
+        " offsetof(ngrav_gpu_stats, p2p_pairs), offsetof(ngrav_gpu_stats, lmac_last_check_rms),"
+        " sizeof(ngrav_gpu_lmac_opts), sizeof(ngrav_gpu_lmac_train_opts), offsetof(ngrav_gpu_lmac_train_opts, seed),"
+        " sizeof(ngrav_gpu_lmac_report));return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(pkg.Opts), ctypes.sizeof(pkg.Diag), ctypes.sizeof(pkg.Ferr), ctypes.sizeof(pkg.Stats),
-            pkg.Opts.G.offset, pkg.Stats.p2p_pairs.offset]
+            pkg.Opts.G.offset, pkg.Stats.p2p_pairs.offset, pkg.Stats.lmac_last_check_rms.offset,
+            ctypes.sizeof(pkg.LmacOpts), ctypes.sizeof(pkg.LmacTrainOpts), pkg.LmacTrainOpts.seed.offset,
+            ctypes.sizeof(pkg.LmacReport)]
     assert got == want
+
+
+def test_lmac_default_opts_without_gpu(pkg):
+    L = pkg.load_library()
+    o = pkg.LmacOpts()
+    assert L.ngrav_gpu_lmac_default_opts(ctypes.byref(o)) == 0
+    assert o.check_every == 10 and o.check_targets == 4096 and o.revert_rms == pytest.approx(1e-3)
+    assert 0.0 < o.rho_lo < o.rho_hi and o.budget > 0.0
+    t = pkg.LmacTrainOpts()
+    assert L.ngrav_gpu_lmac_default_train_opts(ctypes.byref(t)) == 0
+    assert t.snapshots == 16 and t.pairs == 1 << 22 and t.batch % 128 == 0
