@@ -652,8 +652,10 @@ int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp
                             ctx->stream));
     launch_inverse_id(n, ctx->P.id, ctx->inv, ctx->stream);
     launch_gather_slots(ctx->inv, ctx->dtargets, nsample, ctx->dslots, ctx->stream);
+    const int shares = sampler_shares(n, nsample, ctx->sm_count);
+    NG_TRY(ensure_partial(ctx, 3LL * shares * nsample));
     launch_sampler(n, ctx->P, split_of(ctx), ctx->dslots, nsample, ctx->opts.eps * ctx->opts.eps, fp64_pairs != 0,
-                   ctx->dsamp, ctx->stream);
+                   ctx->dsamp, ctx->dpartial, shares, ctx->stream);
     std::vector<double> ref(3 * (size_t)nsample);
     std::vector<int> slots(nsample);
     NG_CUDA(cudaMemcpyAsync(ref.data(), ctx->dsamp, sizeof(double) * 3 * nsample, cudaMemcpyDeviceToHost,

@@ -20,8 +20,11 @@ void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, d
                        cudaStream_t s);
 int potential_blocks(long long n);
 void launch_potential(long long n, const Particles& P, bool split, double eps2, double* partial, cudaStream_t s);
+int sampler_shares(long long n, int nslots, int sm_count);
+// FP64 pairs (one block per target), or FP32 pairs tiled over `shares`
+// source shares with FP64 totals (partial: shares * 3 * nslots doubles).
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
-                    bool fp64_pairs, double* out, cudaStream_t s);
+                    bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s);
 void launch_reset_counters(Counters* C, cudaStream_t s);
 void eval_set_attributes();
 int walk_warps_per_block();

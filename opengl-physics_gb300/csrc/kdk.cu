@@ -359,12 +359,11 @@ void launch_potential(long long n, const Particles& P, bool split, double eps2, 
 }
 
 // ---------------------------------------------------------------------------
-// Direct-sum force-error sampler: one block per target slot.
+// Direct-sum force-error sampler.  FP64 pairs: one block per target slot.
 // ---------------------------------------------------------------------------
 
 constexpr int kSampThreads = 256;
 
-template <bool FP64PAIRS>
 __global__ void __launch_bounds__(kSampThreads) sampler_kernel(long long n, const float4* __restrict__ pos,
                                                                const float4* __restrict__ plo,
                                                                const int* __restrict__ slots, double eps2,
@@ -374,53 +373,24 @@ __global__ void __launch_bounds__(kSampThreads) sampler_kernel(long long n, cons
     const float4 tp = pos[ti];
     const float4 tl = plo ? plo[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
     double ax = 0.0, ay = 0.0, az = 0.0;
-    if (FP64PAIRS) {
-        const double xi = (double)tp.x + (double)tl.x, yi = (double)tp.y + (double)tl.y,
-                     zi = (double)tp.z + (double)tl.z;
-        for (long long j = threadIdx.x; j < n; j += kSampThreads) {
-            if (j == ti) continue;
-            const float4 p = pos[j];
-            double x = p.x, y = p.y, z = p.z;
-            if (plo) {
-                const float4 l = plo[j];
-                x += (double)l.x;
-                y += (double)l.y;
-                z += (double)l.z;
-            }
-            const double dx = x - xi, dy = y - yi, dz = z - zi;
-            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double inv = rsqrt(r2);
-            const double s = (double)p.w * inv * inv * inv;
-            ax += s * dx;
-            ay += s * dy;
-            az += s * dz;
+    const double xi = (double)tp.x + (double)tl.x, yi = (double)tp.y + (double)tl.y, zi = (double)tp.z + (double)tl.z;
+    for (long long j = threadIdx.x; j < n; j += kSampThreads) {
+        if (j == ti) continue;
+        const float4 p = pos[j];
+        double x = p.x, y = p.y, z = p.z;
+        if (plo) {
+            const float4 l = plo[j];
+            x += (double)l.x;
+            y += (double)l.y;
+            z += (double)l.z;
         }
-    } else {
-        const float e2 = (float)eps2;
-        long long j = threadIdx.x;
-        while (j < n) {
-            float px = 0.f, py = 0.f, pz = 0.f;
-            for (int c = 0; c < 64 && j < n; ++c, j += kSampThreads) {
-                if (j == ti) continue;
-                const float4 p = pos[j];
-                float dx = p.x - tp.x, dy = p.y - tp.y, dz = p.z - tp.z;
-                if (plo) {
-                    const float4 l = plo[j];
-                    dx += l.x - tl.x;
-                    dy += l.y - tl.y;
-                    dz += l.z - tl.z;
-                }
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2)));
-                const float inv = rsqrtf(r2);
-                const float f = p.w * inv * inv * inv;
-                px = fmaf(f, dx, px);
-                py = fmaf(f, dy, py);
-                pz = fmaf(f, dz, pz);
-            }
-            ax += px;
-            ay += py;
-            az += pz;
-        }
+        const double dx = x - xi, dy = y - yi, dz = z - zi;
+        const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+        const double inv = rsqrt(r2);
+        const double s = (double)p.w * inv * inv * inv;
+        ax += s * dx;
+        ay += s * dy;
+        az += s * dz;
     }
     const double sx = block_sum_d(ax, red);
     const double sy = block_sum_d(ay, red);
@@ -483,13 +453,91 @@ double run_fma_probe(int sm_count, cudaStream_t s) {
     return 2.0 * fmas / (best * 1e-3) / 1e12;
 }
 
+// FP32 pairs, tiled: a block holds 256 targets (one per thread) and streams
+// one contiguous share of the sources through shared memory; each source tile
+// is summed in FP32 and added to the thread's FP64 totals.  Partial sums per
+// (share, target) are reduced in share order by sampler_reduce_kernel.
+constexpr int kSampTile = 256;
+
+__global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, const float4* __restrict__ pos,
+                                                                 const float4* __restrict__ plo,
+                                                                 const int* __restrict__ slots, int nslots,
+                                                                 float eps2, long long share,
+                                                                 double* __restrict__ partial) {
+    __shared__ float4 sp[kSampTile];
+    __shared__ float4 sl[kSampTile];
+    const int t = blockIdx.x * kSampTile + threadIdx.x;
+    const bool valid = t < nslots;
+    const int ti = valid ? slots[t] : -1;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 tp = valid ? pos[ti] : zero;
+    const float4 tl = (valid && plo) ? plo[ti] : zero;
+    const long long j0 = (long long)blockIdx.y * share;
+    const long long j1 = j0 + share < n ? j0 + share : n;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (long long base = j0; base < j1; base += kSampTile) {
+        const long long j = base + threadIdx.x;
+        sp[threadIdx.x] = j < j1 ? pos[j] : zero;
+        sl[threadIdx.x] = (j < j1 && plo) ? plo[j] : zero;
+        __syncthreads();
+        const int cnt = (int)(j1 - base < kSampTile ? j1 - base : kSampTile);
+        float px = 0.f, py = 0.f, pz = 0.f;
+        for (int k = 0; k < cnt; ++k) {
+            const float4 p = sp[k];
+            const float4 l = sl[k];
+            const float dx = (p.x - tp.x) + (l.x - tl.x);
+            const float dy = (p.y - tp.y) + (l.y - tl.y);
+            const float dz = (p.z - tp.z) + (l.z - tl.z);
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+            const float inv = rsqrtf(r2);
+            const float f = base + k == ti ? 0.f : p.w * inv * inv * inv;
+            px = fmaf(f, dx, px);
+            py = fmaf(f, dy, py);
+            pz = fmaf(f, dz, pz);
+        }
+        ax += px;
+        ay += py;
+        az += pz;
+        __syncthreads();
+    }
+    if (valid) {
+        double* o = partial + ((long long)blockIdx.y * nslots + t) * 3;
+        o[0] = ax;
+        o[1] = ay;
+        o[2] = az;
+    }
+}
+
+__global__ void sampler_reduce_kernel(const double* __restrict__ partial, int nslots, int shares,
+                                      double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * nslots) return;
+    double s = 0.0;
+    for (int k = 0; k < shares; ++k) s += partial[(long long)k * 3 * nslots + i];
+    out[i] = s;
+}
+
+int sampler_shares(long long n, int nslots, int sm_count) {
+    const int tb = (nslots + kSampTile - 1) / kSampTile;
+    long long sh = ((long long)sm_count * 4 + tb - 1) / tb;
+    const long long max_sh = (n + kSampTile - 1) / kSampTile;
+    if (sh > max_sh) sh = max_sh;
+    return (int)(sh < 1 ? 1 : sh);
+}
+
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
-                    bool fp64_pairs, double* out, cudaStream_t s) {
+                    bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s) {
     if (nslots <= 0) return;
-    if (fp64_pairs)
-        sampler_kernel<true><<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
-    else
-        sampler_kernel<false><<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
+    if (fp64_pairs) {
+        sampler_kernel<<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
+        return;
+    }
+    long long share = (n + shares - 1) / shares;
+    share = (share + kSampTile - 1) / kSampTile * kSampTile;
+    const dim3 grid((nslots + kSampTile - 1) / kSampTile, shares);
+    sampler_tiled_kernel<<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots, (float)eps2,
+                                                    share, partial);
+    sampler_reduce_kernel<<<(3 * nslots + 255) / 256, 256, 0, s>>>(partial, nslots, shares, out);
 }
 
 }  // namespace ngrav
