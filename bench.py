@@ -9,12 +9,19 @@ walk with P2P/P2C, closing kick) over the whole system.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-value   = N * K / (device time of the K timed steps, CUDA events on the
-          engine's stream), inputs resident in HBM.
-e2e     = the same metric through the reference-facing C-ABI with host
-          buffers: per step ngrav_gpu_set_particles_f32 from pinned host
-          memory + ngrav_gpu_compute_accel into pinned FP64 host arrays
-          (the ComputeAccelBarnesHut contract), wall clock.
+Headline: the learned opening test against the plain theta test at equal
+rms relative force error (1e-3, FP64-summed direct sum on 4,096 targets).
+Setup, untimed: the network is trained on the run itself (16 snapshots,
+2^22 labelled pairs), theta and the learned budget are each set to the
+largest grid value whose error stays within the target.  Then both arms
+step the same system K times.
+
+value   = N * K / (device time of the learned arm's K timed steps, CUDA
+          events on the engine's stream), inputs resident in HBM; the theta
+          arm's figure and the ratio are in config.
+e2e     = the same metric through the C-ABI with host buffers: per step
+          ngrav_gpu_set_state_f32 from pinned host memory, ngrav_gpu_step(1),
+          ngrav_gpu_get_state into pinned FP64 arrays, wall clock.
 roofline: the evaluation kernel (P2P + P2C, FP32 pipe): algorithmic
           flops (20 per P2P pair + 60 per P2C term, device-counted) / its
           event-timed duration, against the measured FP32 FMA peak.
@@ -165,6 +172,45 @@ def run_reference(args, rank, world):
     return 0
 
 
+THETA_GRID = (0.5, 0.55, 0.6, 0.625, 0.65, 0.675, 0.7, 0.75, 0.8)
+BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 3e-4, 4e-4, 5e-4, 7e-4, 1e-3)
+TARGET_RMS = 1e-3
+
+
+def error_at(sim, seed=2024):
+    """One force evaluation of the current state and its rms / max relative
+    error against the direct sum (FP32 pairs, FP64 sums) on 4,096 targets."""
+    sim.compute_accel()
+    return sim.force_error(nsample=4096, seed=seed, fp64_pairs=False)
+
+
+def calibrate(sim, grid, setter, target=TARGET_RMS):
+    """Largest grid value whose rms error stays within the target."""
+    table, best = [], None
+    for v in grid:
+        setter(v)
+        fe = error_at(sim)
+        table.append([v, fe["rms"], fe["max"]])
+        if fe["rms"] <= target:
+            best = v
+    return (best if best is not None else grid[0]), table
+
+
+def timed(sim, steps, warmup, dt, clocks=None):
+    sim.step(warmup, dt)
+    if clocks:
+        clocks.start()
+    sim.reset_cumulative()
+    sim.step(steps, dt)
+    st = sim.stats()
+    clk = clocks.stop() if clocks else None
+    return st, st["cum_ms_step"] / steps, clk
+
+
+def phases(st):
+    return {k: st[k] for k in ("ms_bbox_keys", "ms_sort", "ms_build", "ms_moments", "ms_walk", "ms_force")}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -172,7 +218,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="galaxy4m", choices=sorted(WORKLOADS))
-    ap.add_argument("--theta", type=float, default=None)
+    ap.add_argument("--mac", default="learned", choices=["learned", "geometric"],
+                    help="learned: train, calibrate both tests to the target rms, time both arms")
+    ap.add_argument("--theta", type=float, default=None, help="geometric arm theta (default: calibrated)")
+    ap.add_argument("--budget", type=float, default=None, help="learned arm budget (default: calibrated)")
+    ap.add_argument("--lmac-pairs", type=int, default=1 << 22)
+    ap.add_argument("--lmac-snapshots", type=int, default=16)
     ap.add_argument("--precision", default="split", choices=["split", "plain"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -184,16 +235,37 @@ def main():
     pkg = ge.load_package()
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"])
     dev = local
-    arrs, eps, dt, theta, ncrit = make_inputs(ic, args.workload)
-    if args.theta is not None:
-        theta = args.theta
+    arrs, eps, dt, theta0, ncrit = make_inputs(ic, args.workload)
     n = len(arrs[0])
     prec = pkg.PRECISION_SPLIT if args.precision == "split" else pkg.PRECISION_PLAIN
-    sim = pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=ncrit, precision=prec,
+    sim = pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta0, dt=dt), leaf_capacity=ncrit, precision=prec,
                           device=dev, timing=True)
     sim.set_particles_f32(*arrs)
     sim.prime()
-    sim.step(args.warmup, dt)
+    learned = args.mac == "learned"
+
+    # ---- setup (untimed): train on the run itself, calibrate both tests ----
+    train, cal_theta, cal_budget = None, None, None
+    if learned:
+        t0 = time.perf_counter()
+        train = sim.lmac_train(snapshots=args.lmac_snapshots, steps_between=1, dt=dt, pairs=args.lmac_pairs,
+                               epochs=4, batch=8192, seed=1)
+        train["wall_s"] = time.perf_counter() - t0
+    if args.theta is None:
+        theta, cal_theta = calibrate(sim, THETA_GRID, lambda v: sim.set_opts(theta=v, mac=pkg.MAC_GEOMETRIC))
+    else:
+        theta = args.theta
+    sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
+    budget = None
+    if learned:
+        def set_budget(v):
+            sim.set_opts(mac=pkg.MAC_LEARNED)
+            sim.lmac_set_opts(budget=v, check_every=0)
+        if args.budget is None:
+            budget, cal_budget = calibrate(sim, BUDGET_GRID, set_budget)
+        else:
+            budget = args.budget
+
     dist = None
     if world > 1:
         import torch
@@ -203,12 +275,28 @@ def main():
         dist = tdist
         dist.barrier()
     clocks = ClockSampler(dev)
-    clocks.start()
-    sim.reset_cumulative()
-    sim.step(args.steps, dt)
-    st = sim.stats()
-    clk = clocks.stop()
-    ms_step = st["cum_ms_step"] / args.steps
+
+    # ---- geometric (plain theta) arm ----
+    sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
+    st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks)
+    fe_g = error_at(sim)
+    arm_theta = {"theta": theta, "value": world * n / (ms_g * 1e-3), "ms_per_step": ms_g,
+                 "force_err_rms": fe_g["rms"], "force_err_max": fe_g["max"],
+                 "p2p_pairs_per_step": st_g["cum_p2p_pairs"] / max(1, st_g["cum_evals"]),
+                 "p2c_terms_per_step": st_g["cum_p2c_terms"] / max(1, st_g["cum_evals"]),
+                 "ms_walk_per_step": st_g["cum_ms_walk"] / max(1, st_g["cum_evals"]),
+                 "ms_force_per_step": st_g["cum_ms_force"] / max(1, st_g["cum_evals"]),
+                 "ms_phases_last_eval": phases(st_g), "calibration": cal_theta}
+
+    # ---- learned arm (the method) ----
+    if learned:
+        sim.set_opts(mac=pkg.MAC_LEARNED)
+        sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=TARGET_RMS * 1.5)
+        sim.lmac_reset()
+        st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks)
+        fe = error_at(sim)
+    else:
+        st, ms_step, clk, fe = st_g, ms_g, clk_g, fe_g
     ms_max = ms_step
     if dist is not None:
         import torch
@@ -217,44 +305,44 @@ def main():
         ms_max = float(t.item())
     value = world * n / (ms_max * 1e-3)
 
-    # roofline of the walk kernel
+    # roofline of the evaluation kernel (P2P + P2C on the FP32 pipe)
     flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
     force_s = st["cum_ms_force"] * 1e-3
     achieved = flops / force_s / 1e12 if force_s > 0 else None
     peak = pkg.probe_fp32_peak(dev)
-    force = sim.force_error(nsample=4096, seed=2024, fp64_pairs=False)
 
-    # e2e: host buffers through the C-ABI, wall clock
-    e2e = None
-    h2d = 7 * 4 * n
-    d2h = 3 * 8 * n
+    # e2e through the C-ABI with host buffers: each step writes the state from
+    # pinned host memory (ngrav_gpu_set_state_f32), runs one KDK step and reads
+    # positions and velocities back (ngrav_gpu_get_state), wall clock.
+    import ctypes
     try:
         import torch
-        pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() for a in arrs]
-        outs = [torch.empty(n, dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        hin = [pin(a.astype(np.float32)) for a in sim.state()]
+        hout = [torch.empty(n, dtype=torch.float64).pin_memory().numpy() for _ in range(6)]
     except Exception:
-        pinned = [np.ascontiguousarray(a) for a in arrs]
-        outs = [np.empty(n) for _ in range(3)]
-    x0 = sim.state()  # keep the stepped state for reporting
-    del x0
-    import ctypes
-    fptr = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) for a in pinned]
-    dptr = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in outs]
+        hin = [np.ascontiguousarray(a, dtype=np.float32) for a in sim.state()]
+        hout = [np.empty(n) for _ in range(6)]
+    fin = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) for a in hin]
+    dout = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in hout]
     L = sim.L
     t_e2e = []
     for k in range(1 + args.e2e_steps):
         t0 = time.perf_counter()
-        rc = L.ngrav_gpu_set_particles_f32(sim.h, n, *fptr)
-        rc |= L.ngrav_gpu_compute_accel(sim.h, *dptr)
+        rc = L.ngrav_gpu_set_state_f32(sim.h, *fin)
+        rc |= L.ngrav_gpu_step(sim.h, 1, ctypes.c_double(dt))
+        rc |= L.ngrav_gpu_get_state(sim.h, *dout)
         t1 = time.perf_counter()
         if rc:
             raise RuntimeError("e2e call failed: " + L.ngrav_gpu_last_error(sim.h).decode())
         if k > 0:
             t_e2e.append(t1 - t0)
+        for a, b in zip(hin, hout):
+            a[:] = b  # the next step starts from this step's result
     e2e_ms = 1e3 * float(np.mean(t_e2e))
-    e2e = {"value": world * n / (e2e_ms * 1e-3), "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-           "call": "ngrav_gpu_set_particles_f32 + ngrav_gpu_compute_accel (pinned host buffers)"}
+    e2e = {"value": world * n / (e2e_ms * 1e-3), "unit": "particle-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
+           "d2h_bytes_per_step": 6 * 8 * n, "ms_per_step": e2e_ms,
+           "call": "ngrav_gpu_set_state_f32 + ngrav_gpu_step(1) + ngrav_gpu_get_state (pinned host buffers)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -264,28 +352,37 @@ def main():
             cpu = {"error": str(exc)}
 
     if rank == 0:
+        cfg = {"workload": args.workload, "n": n, "mac": args.mac, "eps": eps, "dt": dt, "leaf_capacity": ncrit,
+               "precision": args.precision, "quadrupole": True, "target_rms": TARGET_RMS,
+               "parallelism": "replicas" if world > 1 else "single-gpu",
+               "l2": "per-step working set > 0.5 GB, larger than the 129 MB L2",
+               "force_err_rms": fe["rms"], "force_err_max": fe["max"], "force_err_median": fe["median"],
+               "force_err_targets": fe["nsample"],
+               "interactions_per_s": (st["cum_p2p_pairs"] + st["cum_p2c_terms"]) / (st["cum_ms_step"] * 1e-3),
+               "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
+               "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
+               "ms_walk_per_step": st["cum_ms_walk"] / max(1, st["cum_evals"]),
+               "ms_force_per_step": st["cum_ms_force"] / max(1, st["cum_evals"]),
+               "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"]),
+               "list_entries_per_step": st["far_entries"] + st["near_entries"],
+               "mac_tests_per_step": st["mac_tests"], "walk_stack_max": st["walk_stack_max"],
+               "leaves": st["leaves"], "nodes": st["nodes"], "ms_phases_last_eval": phases(st),
+               "graph_replays": st["graph_replays"], "theta_arm": arm_theta}
+        if learned:
+            cfg["learned"] = {"budget": budget, "calibration": cal_budget, "train": train,
+                              "queries_last_eval": st["lmac_queries"], "accepts_last_eval": st["lmac_accepts"],
+                              "fallbacks_last_eval": st["lmac_fallbacks"], "screened_last_eval": st["lmac_screened"],
+                              "tensor_flushes_last_eval": st["lmac_flushes"],
+                              "mlp_flops_last_eval": 2624.0 * st["lmac_queries"],
+                              "checks": st["lmac_checks"], "last_check_rms": st["lmac_last_check_rms"],
+                              "reverted": bool(st["lmac_reverted"])}
+            cfg["speedup_vs_theta_arm"] = value / arm_theta["value"]
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
-            "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded galaxy generator)" if args.workload == "galaxy4m" else "synthetic",
-            "config": {"workload": args.workload, "n": n, "mac": "geometric", "theta": theta, "eps": eps, "dt": dt,
-                       "leaf_capacity": ncrit, "precision": args.precision, "quadrupole": True,
-                       "parallelism": "replicas" if world > 1 else "single-gpu",
-                       "l2": "per-step working set > 0.5 GB, larger than the 129 MB L2",
-                       "force_err_rms": force["rms"], "force_err_max": force["max"],
-                       "force_err_median": force["median"], "force_err_targets": force["nsample"],
-                       "interactions_per_s": (st["cum_p2p_pairs"] + st["cum_p2c_terms"]) / (st["cum_ms_step"] * 1e-3),
-                       "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
-                       "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
-                       "ms_walk_per_step": st["cum_ms_walk"] / max(1, st["cum_evals"]),
-                       "ms_force_per_step": st["cum_ms_force"] / max(1, st["cum_evals"]),
-                       "list_entries_per_step": st["far_entries"] + st["near_entries"],
-                       "mac_tests_per_step": st["mac_tests"], "mac_retests_per_step": st["mac_retests"],
-                       "walk_stack_max": st["walk_stack_max"], "leaves": st["leaves"], "nodes": st["nodes"],
-                       "ms_phases_last_eval": {k: st[k] for k in ("ms_bbox_keys", "ms_sort", "ms_build",
-                                                                  "ms_moments", "ms_walk", "ms_force")},
-                       "ms_eval_per_step": st["cum_ms_eval"] / max(1, st["cum_evals"])},
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded galaxy generator)" if args.workload.startswith("galaxy") else "synthetic",
+            "config": cfg,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved and peak else None,
                          "traffic": EVAL_DRAM_BYTES_PER_LIST_ENTRY * (st["far_entries"] + st["near_entries"]),

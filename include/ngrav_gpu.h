@@ -123,11 +123,13 @@ typedef struct ngrav_gpu_stats {
     int list_max;          /* longest per-group list */
     /* learned opening test, last evaluation: pairs handed to the network,
      * accepted by it, decided by the geometric fallback (low confidence);
-     * tensor-core flushes; whether it ran, whether the run reverted to the
+     * tensor-core flushes; band pairs the error bound accepted unasked; whether it ran, whether the run reverted to the
      * geometric test, checks made and the last checked rms error */
-    long long lmac_queries, lmac_accepts, lmac_fallbacks, lmac_flushes;
+    long long lmac_queries, lmac_accepts, lmac_fallbacks, lmac_flushes, lmac_screened;
     int lmac_active, lmac_reverted, lmac_checks;
     double lmac_last_check_rms;
+    /* KDK steps launched as a captured CUDA graph: captures made, replays */
+    long long graph_captures, graph_replays;
 } ngrav_gpu_stats;
 
 typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;
@@ -154,6 +156,16 @@ int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, cons
 /* FP32 variant: no conversion, for large N. */
 int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
                                 const float* vx, const float* vy, const float* vz, const float* m);
+
+/* New positions (and velocities, unless NULL) for the particles already set,
+ * in the caller's order; masses stay, and so do the accelerations of the last
+ * evaluation (the next KDK step's opening kick and the learned test's
+ * per-group scale use them).  Writes through System<3>::MutableState
+ * (include/ngrav/System.hpp:197) on an unchanged particle set. */
+int ngrav_gpu_set_state(ngrav_gpu_ctx* ctx, const double* x, const double* y, const double* z, const double* vx,
+                        const double* vy, const double* vz);
+int ngrav_gpu_set_state_f32(ngrav_gpu_ctx* ctx, const float* x, const float* y, const float* z, const float* vx,
+                            const float* vy, const float* vz);
 
 /* One force evaluation on the current positions, written in the caller's
  * original particle order, G included -- the contract of
@@ -246,6 +258,11 @@ typedef struct ngrav_gpu_lmac_opts {
     int check_every;       /* evaluations between FP64 checks (0: never) */
     int check_targets;     /* sampled targets of one check */
     double revert_rms;     /* rms relative force error that triggers the revert */
+    int rounds;            /* walk rounds, 2..8: pairs for the network are decided between
+                            * rounds; the last round decides them geometrically */
+    double screen;         /* accept a band pair without the network when the quadrupole
+                            * truncation bound on its error is at most screen x budget
+                            * (0: every band pair goes to the network) */
 } ngrav_gpu_lmac_opts;
 
 typedef struct ngrav_gpu_lmac_train_opts {

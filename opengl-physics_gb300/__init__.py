@@ -38,6 +38,7 @@ PRECISION_PLAIN, PRECISION_SPLIT = 0, 1
 EXPORTS = (
     "ngrav_gpu_default_opts", "ngrav_gpu_create", "ngrav_gpu_destroy", "ngrav_gpu_last_error",
     "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
+    "ngrav_gpu_set_state", "ngrav_gpu_set_state_f32",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
@@ -85,8 +86,10 @@ class Stats(ctypes.Structure):
                 ("far_entries", ctypes.c_longlong), ("near_entries", ctypes.c_longlong), ("list_max", ctypes.c_int),
                 ("lmac_queries", ctypes.c_longlong), ("lmac_accepts", ctypes.c_longlong),
                 ("lmac_fallbacks", ctypes.c_longlong), ("lmac_flushes", ctypes.c_longlong),
+                ("lmac_screened", ctypes.c_longlong),
                 ("lmac_active", ctypes.c_int), ("lmac_reverted", ctypes.c_int), ("lmac_checks", ctypes.c_int),
-                ("lmac_last_check_rms", ctypes.c_double)]
+                ("lmac_last_check_rms", ctypes.c_double), ("graph_captures", ctypes.c_longlong),
+                ("graph_replays", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -95,7 +98,7 @@ class Stats(ctypes.Structure):
 class LmacOpts(ctypes.Structure):
     _fields_ = [("budget", ctypes.c_double), ("gate", ctypes.c_double), ("rho_lo", ctypes.c_double),
                 ("rho_hi", ctypes.c_double), ("check_every", ctypes.c_int), ("check_targets", ctypes.c_int),
-                ("revert_rms", ctypes.c_double)]
+                ("revert_rms", ctypes.c_double), ("rounds", ctypes.c_int), ("screen", ctypes.c_double)]
 
 
 class LmacTrainOpts(ctypes.Structure):
@@ -161,6 +164,8 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_set_particles.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [_D] * 7
     L.ngrav_gpu_set_particles_f32.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [_F] * 7
     L.ngrav_gpu_compute_accel.argtypes = [ctypes.c_void_p, _D, _D, _D]
+    L.ngrav_gpu_set_state.argtypes = [ctypes.c_void_p] + [_D] * 6
+    L.ngrav_gpu_set_state_f32.argtypes = [ctypes.c_void_p] + [_F] * 6
     L.ngrav_gpu_prime.argtypes = [ctypes.c_void_p]
     L.ngrav_gpu_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
     L.ngrav_gpu_get_state.argtypes = [ctypes.c_void_p] + [_D] * 6
@@ -303,6 +308,12 @@ class NBodySystem:
         arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, vx, vy, vz, m)]
         self.n = len(arrs[0])
         self._check(self.L.ngrav_gpu_set_particles_f32(self.h, self.n, *[_p(a, _F) for a in arrs]), self.h)
+
+    def set_state(self, x, y, z, vx=None, vy=None, vz=None):
+        """New positions / velocities of the current particles (masses and the
+        carried accelerations stay)."""
+        arrs = [_c64(a) for a in (x, y, z, vx, vy, vz)]
+        self._check(self.L.ngrav_gpu_set_state(self.h, *[_p(a, _D) for a in arrs]), self.h)
 
     def compute_accel(self):
         ax, ay, az = (np.empty(self.n) for _ in range(3))

@@ -175,7 +175,11 @@ WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
 }
 
 void rec(ngrav_gpu_ctx* ctx, int i) {
-    if (ctx->events) cudaEventRecord(ctx->ev[i], ctx->stream);
+    if (!ctx->events) return;
+    if (ctx->capturing)  // a timing node of the captured graph
+        cudaEventRecordWithFlags(ctx->ev[i], ctx->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(ctx->ev[i], ctx->stream);
 }
 
 // Enqueue one force evaluation. bbox_ready: the counters were reset and the
@@ -242,6 +246,11 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
         return NGRAV_OK;
     }
     if (st & kStCorrupt) return fail(ctx, NGRAV_ERR_CAPACITY, "walk visit limit breached (inconsistent tree)");
+    if (st & kStPendOverflow) {
+        NG_TRY(lmac_grow_pools(ctx));
+        retry = true;
+        return NGRAV_OK;
+    }
     if (st & kStStackOverflow) {
         if (!ctx->walk_global_stack) {
             ctx->walk_global_stack = true;  // the shared-memory stack was too small for this tree
@@ -293,6 +302,7 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
 int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
     for (int attempt = 0; attempt < 8; ++attempt) {
+        lmac_prepare(ctx);
         enqueue_eval(ctx, bbox_ready, kick, hdt);
         bool retry = false;
         NG_TRY(finish_eval(ctx, retry));
@@ -369,6 +379,127 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
     return NGRAV_OK;
 }
 
+// Everything the launches of one KDK step bake in: buffers, sizes,
+// parameters, the walk variant.  Equal keys replay the same graph.
+std::vector<unsigned char> step_key(const ngrav_gpu_ctx* ctx, float hdt, float fdt) {
+    std::vector<unsigned char> k;
+    k.reserve(1024);
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        k.insert(k.end(), b, b + n);
+    };
+    put(&ctx->P, sizeof(ctx->P));
+    put(&ctx->T, sizeof(ctx->T));
+    put(&ctx->SB, sizeof(ctx->SB));
+    put(&ctx->LB, sizeof(ctx->LB));
+    put(&ctx->C, sizeof(ctx->C));
+    put(&ctx->leaf_at, sizeof(ctx->leaf_at));
+    put(&ctx->flags, sizeof(ctx->flags));
+    put(&ctx->scanbuf, sizeof(ctx->scanbuf));
+    put(&ctx->leaf_list, sizeof(ctx->leaf_list));
+    put(&ctx->n, sizeof(ctx->n));
+    put(&ctx->opts, sizeof(ctx->opts));
+    put(&ctx->walk_global_stack, sizeof(ctx->walk_global_stack));
+    put(&ctx->eval_nwarps, sizeof(ctx->eval_nwarps));
+    put(&ctx->events, sizeof(ctx->events));
+    put(&hdt, sizeof(hdt));
+    put(&fdt, sizeof(fdt));
+    lmac_key(ctx, k);
+    return k;
+}
+
+void drop_graphs(ngrav_gpu_ctx* ctx) {
+    for (auto& g : ctx->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.key.clear();
+    }
+}
+
+// Enqueue one KDK step (kick-drift + evaluation with the closing kick) as a
+// graph launch: replayed when a graph with the same key exists, else
+// captured first.  Returns false (nothing enqueued) if capture failed; the
+// caller then launches directly.
+bool enqueue_step_graph(ngrav_gpu_ctx* ctx, float hdt, float fdt) {
+    lmac_prepare(ctx);
+    std::vector<unsigned char> key = step_key(ctx, hdt, fdt);
+    for (auto& g : ctx->graphs) {
+        if (g.exec && g.key == key) {
+            if (cudaGraphLaunch(g.exec, ctx->stream) != cudaSuccess) return false;
+            // the host side of the step the graph replays
+            const void* model = nullptr;
+            WalkParams wp = walk_params(ctx, true, hdt);
+            lmac_walk_setup(ctx, wp, &model);
+            std::swap(ctx->P.pos, ctx->P.pos2);
+            std::swap(ctx->P.plo, ctx->P.plo2);
+            std::swap(ctx->P.vel, ctx->P.vel2);
+            std::swap(ctx->P.acc, ctx->P.acc2);
+            std::swap(ctx->P.id, ctx->P.id2);
+            ctx->launches += g.launches;
+            ctx->graph_replays += 1;
+            return true;
+        }
+    }
+    Particles saved = ctx->P;
+    const long long launches0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    ctx->capturing = true;
+    launch_reset_counters(ctx->C, ctx->stream);
+    launch_kick_drift(ctx->P, ctx->n, hdt, fdt, split_of(ctx), ctx->C, ctx->stream);
+    ctx->launches += 2;
+    enqueue_eval(ctx, true, true, hdt);
+    ctx->capturing = false;
+    const cudaError_t e1 = cudaStreamEndCapture(ctx->stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e2 = (e1 == cudaSuccess) ? cudaGraphInstantiate(&exec, graph, 0) : e1;
+    if (graph) cudaGraphDestroy(graph);
+    if (e2 != cudaSuccess || cudaGraphLaunch(exec, ctx->stream) != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGetLastError();
+        ctx->P = saved;  // nothing ran: undo the host side of the captured step
+        ctx->launches = launches0;
+        ctx->use_graphs = false;
+        return false;
+    }
+    auto& slot = ctx->graphs[ctx->graph_next];
+    ctx->graph_next ^= 1;
+    if (slot.exec) cudaGraphExecDestroy(slot.exec);
+    slot.exec = exec;
+    slot.key = std::move(key);
+    slot.launches = ctx->launches - launches0;
+    ctx->graph_captures += 1;
+    return true;
+}
+
+template <typename T>
+int set_state_impl(ngrav_gpu_ctx* ctx, const T* x, const T* y, const T* z, const T* vx, const T* vy, const T* vz,
+                   bool f64) {
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    if (!x || !y || !z) return fail(ctx, NGRAV_ERR_INVALID_ARG, "NULL position array");
+    const bool have_v = vx && vy && vz;
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    T* st = reinterpret_cast<T*>(ctx->stage);
+    const size_t b = sizeof(T) * (size_t)n;
+    const T* srcs[6] = {x, y, z, vx, vy, vz};
+    for (int k = 0; k < (have_v ? 6 : 3); ++k)
+        NG_CUDA(cudaMemcpyAsync(st + (size_t)k * n, srcs[k], b, cudaMemcpyHostToDevice, ctx->stream));
+    const T* v[3] = {have_v ? st + 3 * (size_t)n : nullptr, have_v ? st + 4 * (size_t)n : nullptr,
+                     have_v ? st + 5 * (size_t)n : nullptr};
+    if (f64)
+        launch_state_f64(n, (const double*)st, (const double*)(st + n), (const double*)(st + 2 * n),
+                         (const double*)v[0], (const double*)v[1], (const double*)v[2], ctx->P, split_of(ctx),
+                         ctx->stream);
+    else
+        launch_state_f32(n, (const float*)st, (const float*)(st + n), (const float*)(st + 2 * n), (const float*)v[0],
+                         (const float*)v[1], (const float*)v[2], ctx->P, split_of(ctx), ctx->stream);
+    ctx->launches += 1;
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    NG_CUDA(cudaGetLastError());
+    return NGRAV_OK;
+}
+
 }  // namespace ngrav_ctx
 
 using namespace ngrav_ctx;
@@ -411,6 +542,7 @@ int ngrav_gpu_create(ngrav_gpu_ctx** out, const ngrav_gpu_opts* opts) {
         NG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
         NG_CUDA(cudaMalloc((void**)&ctx->C, sizeof(Counters)));
         eval_set_attributes();
+        lmac_set_attributes();
         NG_CUDA(cudaGetLastError());
         // Walk: up to 32 resident warps per SM (latency-bound traversal);
         // evaluation: every warp the occupancy calculator allows.
@@ -437,6 +569,7 @@ void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->opts.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graphs(ctx);
     lmac_destroy(ctx);
     free_particles(ctx);
     free_nodes(ctx);
@@ -496,6 +629,19 @@ int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, c
     return set_particles_impl<float>(ctx, n, x, y, z, vx, vy, vz, m, false);
 }
 
+
+int ngrav_gpu_set_state(ngrav_gpu_ctx* ctx, const double* x, const double* y, const double* z, const double* vx,
+                        const double* vy, const double* vz) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    return set_state_impl<double>(ctx, x, y, z, vx, vy, vz, true);
+}
+
+int ngrav_gpu_set_state_f32(ngrav_gpu_ctx* ctx, const float* x, const float* y, const float* z, const float* vx,
+                            const float* vy, const float* vz) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    return set_state_impl<float>(ctx, x, y, z, vx, vy, vz, false);
+}
+
 int ngrav_gpu_compute_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az) {
     if (!ctx) return NGRAV_ERR_INVALID_ARG;
     if (!ax || !ay || !az) return fail(ctx, NGRAV_ERR_INVALID_ARG, "NULL output array");
@@ -529,6 +675,18 @@ int ngrav_gpu_step(ngrav_gpu_ctx* ctx, int nsteps, double dt) {
     const float hdt = (float)(0.5 * dt), fdt = (float)dt;
     NG_CUDA(cudaEventRecord(ctx->sev[0], ctx->stream));
     for (int k = 0; k < nsteps; ++k) {
+        if (ctx->use_graphs && enqueue_step_graph(ctx, hdt, fdt)) {
+            bool retry = false;
+            NG_TRY(finish_eval(ctx, retry));
+            if (retry) {
+                // capacities grew: redo this step's evaluation directly (the
+                // kick-drift has run; the evaluation starts from its state)
+                NG_TRY(evaluate(ctx, false, true, hdt));
+            } else {
+                NG_TRY(lmac_after_eval(ctx));
+            }
+            continue;
+        }
         launch_reset_counters(ctx->C, ctx->stream);
         launch_kick_drift(ctx->P, ctx->n, hdt, fdt, split_of(ctx), ctx->C, ctx->stream);
         ctx->launches += 2;
@@ -727,6 +885,8 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->cum_ms_eval = ctx->cum_ms_eval;
     out->cum_ms_step = ctx->cum_ms_step;
     out->cum_launches = ctx->launches;
+    out->graph_captures = ctx->graph_captures;
+    out->graph_replays = ctx->graph_replays;
     lmac_fill_stats(ctx, out);
     return NGRAV_OK;
 }

@@ -9,6 +9,7 @@
 #include "engine.cuh"
 
 #include <string>
+#include <vector>
 
 using namespace ngrav;
 
@@ -56,6 +57,19 @@ struct ngrav_gpu_ctx {
     long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
     double cum_ms_walk = 0.0, cum_ms_force = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
     bool acc_valid = false;           // P.acc holds a force evaluation of this particle set
+    // CUDA graphs of one KDK step (kick-drift + force evaluation), keyed by
+    // every pointer and parameter the launches bake in; two slots because the
+    // particle buffers alternate between steps.
+    struct StepGraph {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0;
+    };
+    StepGraph graphs[2];
+    int graph_next = 0;
+    bool capturing = false;
+    bool use_graphs = true;
+    long long graph_captures = 0, graph_replays = 0;
     // learned opening test (model, training buffers, run-time control)
     ngrav_ctx::LmacState* lm = nullptr;
 };
@@ -96,9 +110,16 @@ int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt);
 
 // Learned opening test hooks (lmac_host.cu).
 void lmac_destroy(ngrav_gpu_ctx* ctx);
-// True when the next walk uses the learned test; fills the walk parameters.
+// Decide whether the next walk uses the learned test and put its buffers in
+// place (allocations happen here, never inside a graph capture).
+bool lmac_prepare(ngrav_gpu_ctx* ctx);
+// Fill the walk parameters of a prepared learned walk; false if not prepared.
 bool lmac_walk_setup(ngrav_gpu_ctx* ctx, ngrav::WalkParams& wp, const void** model);
+// Append what a captured step depends on to a graph key.
+void lmac_key(const ngrav_gpu_ctx* ctx, std::vector<unsigned char>& key);
 void lmac_launch_walk(ngrav_gpu_ctx* ctx, const ngrav::WalkParams& wp, const void* model);
+// The deferred-pair pools overflowed: size them to what the walk counted.
+int lmac_grow_pools(ngrav_gpu_ctx* ctx);
 // After a force evaluation: run the periodic FP64 check, revert on a breach.
 int lmac_after_eval(ngrav_gpu_ctx* ctx);
 void lmac_fill_stats(const ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out);

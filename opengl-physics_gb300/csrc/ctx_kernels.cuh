@@ -8,6 +8,10 @@ namespace ngrav {
 void launch_upload_f64(long long n, const double* x, const double* y, const double* z, const double* vx,
                        const double* vy, const double* vz, const double* m, const Particles& P, bool split,
                        cudaStream_t s);
+void launch_state_f64(long long n, const double* x, const double* y, const double* z, const double* vx,
+                      const double* vy, const double* vz, const Particles& P, bool split, cudaStream_t s);
+void launch_state_f32(long long n, const float* x, const float* y, const float* z, const float* vx,
+                      const float* vy, const float* vz, const Particles& P, bool split, cudaStream_t s);
 void launch_upload_f32(long long n, const float* x, const float* y, const float* z, const float* vx,
                        const float* vy, const float* vz, const float* m, const Particles& P, bool split,
                        cudaStream_t s);
@@ -27,6 +31,7 @@ void launch_sampler(long long n, const Particles& P, bool split, const int* slot
                     bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s);
 void launch_reset_counters(Counters* C, cudaStream_t s);
 void eval_set_attributes();
+void lmac_set_attributes();
 int walk_warps_per_block();
 int walk_blocks_per_sm();
 int eval_warps_per_block();

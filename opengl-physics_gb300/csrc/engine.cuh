@@ -33,7 +33,9 @@ enum : unsigned {
     kStTimeout = 16u,
     kStListOverflow = 32u,  // per-warp list staging or the final list pool
     kStCorrupt = 64u,       // walk visit limit breached
-    kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout | kStListOverflow | kStCorrupt,
+    kStPendOverflow = 128u, // learned walk: deferred-pair pool exhausted
+    kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout | kStListOverflow | kStCorrupt |
+               kStPendOverflow,
 };
 
 // Per-evaluation device counters (zeroed before each force evaluation).
@@ -70,6 +72,7 @@ struct Counters {
     unsigned long long lm_accepts;
     unsigned long long lm_fallbacks;
     unsigned long long lm_flushes;
+    unsigned long long lm_screened;   // band pairs the error bound accepted without the network
 };
 
 // Per-group interaction lists written by the walk, read by the evaluation.
@@ -171,6 +174,9 @@ struct WalkParams {
     float lm_log2b;                   // log2 of the per-target error budget
     float lm_gate;                    // |logit| below which the geometric test decides
     float lm_rho_lo, lm_rho_hi;       // band of 2h/worst handed to the network
+    float lm_mu[8], lm_isd[8];        // feature standardisation of the network
+    float lm_screen;                  // accept unasked when the error bound <= lm_screen * budget (0: off)
+    float lm_budget;                  // the budget itself
 };
 
 // ---- launchers (each enqueues on `s`; no host synchronisation) ----

@@ -42,6 +42,23 @@ __global__ void upload_kernel(long long n, const T* __restrict__ x, const T* __r
     }
 }
 
+// New positions / velocities for the current particles, in the caller's
+// order: slot k takes particle id[k]'s values; masses, order and the carried
+// accelerations stay.
+template <typename T>
+__global__ void state_kernel(long long n, const T* __restrict__ x, const T* __restrict__ y,
+                             const T* __restrict__ z, const T* __restrict__ vx, const T* __restrict__ vy,
+                             const T* __restrict__ vz, Particles P, int split) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const int i = P.id[k];
+        const double dx = (double)x[i], dy = (double)y[i], dz = (double)z[i];
+        const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
+        P.pos[k] = make_float4(hx, hy, hz, P.pos[k].w);
+        if (split) P.plo[k] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
+        if (vx) P.vel[k] = make_float4((float)vx[i], (float)vy[i], (float)vz[i], 0.f);
+    }
+}
+
 static unsigned grid_for(long long n, int threads, int max_blocks) {
     long long b = (n + threads - 1) / threads;
     if (b > max_blocks) b = max_blocks;
@@ -59,6 +76,16 @@ void launch_upload_f32(long long n, const float* x, const float* y, const float*
                        const float* vy, const float* vz, const float* m, const Particles& P, bool split,
                        cudaStream_t s) {
     upload_kernel<float><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, x, y, z, vx, vy, vz, m, P, split ? 1 : 0);
+}
+
+void launch_state_f64(long long n, const double* x, const double* y, const double* z, const double* vx,
+                      const double* vy, const double* vz, const Particles& P, bool split, cudaStream_t s) {
+    state_kernel<double><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, x, y, z, vx, vy, vz, P, split ? 1 : 0);
+}
+
+void launch_state_f32(long long n, const float* x, const float* y, const float* z, const float* vx,
+                      const float* vy, const float* vz, const Particles& P, bool split, cudaStream_t s) {
+    state_kernel<float><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, x, y, z, vx, vy, vz, P, split ? 1 : 0);
 }
 
 // out[id[k]] = value of slot k, as FP64, for positions (hi + lo), velocities

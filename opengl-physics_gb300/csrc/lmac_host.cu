@@ -16,13 +16,6 @@
 #include <random>
 #include <vector>
 
-namespace ngrav {
-void launch_walk_lmac(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
-                      const ListBuffers& LB, const LmacDev* model, cudaStream_t s);
-void launch_lmac_tc_forward(const LmacDev* model, const float* X, int n, float* z, unsigned* status, int sm_count,
-                            cudaStream_t s);
-}  // namespace ngrav
-
 namespace ngrav_ctx {
 
 struct LmacState {
@@ -52,7 +45,11 @@ struct LmacState {
     unsigned* dStatus = nullptr;
     float* dZ = nullptr;
     int z_cap = 0;
+    // round-based walk buffers
+    LmacRounds R{};
+    long long gs_cap = 0;
     // run-time control
+    bool prepared = false;    // the next walk uses the learned test (buffers in place)
     bool used_last = false;
     int evals_since_check = 0;
     bool reverted = false;
@@ -241,6 +238,57 @@ int grad_pass(ngrav_gpu_ctx* ctx, const float* P, int nb, float scale, bool step
     return NGRAV_OK;
 }
 
+void free_rounds(LmacState& L) {
+    dfree(L.R.gs);
+    for (int k = 0; k < 2; ++k) {
+        dfree(L.R.active[k]);
+        dfree(L.R.pend_node[k]);
+        dfree(L.R.pend_feat[k]);
+        dfree(L.R.pend_next[k]);
+        dfree(L.R.pend_owner[k]);
+        dfree(L.R.pend_fill[k]);
+    }
+    dfree(L.R.dec);
+    dfree(L.R.ctr);
+    L.R.pend_chunk_cap = 0;
+    L.gs_cap = 0;
+}
+
+// Group state and active lists for `groups` groups; deferred-pair pools of
+// `chunks` chunks each.
+int ensure_rounds(ngrav_gpu_ctx* ctx, long long groups, long long chunks) {
+    LmacState& L = *ctx->lm;
+    if (!L.R.ctr) NG_CUDA(dalloc(L.R.ctr, 4 * kLmMaxRounds));
+    if (groups > L.gs_cap) {
+        dfree(L.R.gs);
+        dfree(L.R.active[0]);
+        dfree(L.R.active[1]);
+        NG_CUDA(dalloc(L.R.gs, groups));
+        NG_CUDA(dalloc(L.R.active[0], groups));
+        NG_CUDA(dalloc(L.R.active[1], groups));
+        L.gs_cap = groups;
+    }
+    chunks = std::min<long long>(chunks, 0x7FFFFFF0LL / kListChunk);
+    if (chunks > L.R.pend_chunk_cap) {
+        for (int k = 0; k < 2; ++k) {
+            dfree(L.R.pend_node[k]);
+            dfree(L.R.pend_feat[k]);
+            dfree(L.R.pend_next[k]);
+            dfree(L.R.pend_owner[k]);
+            dfree(L.R.pend_fill[k]);
+            NG_CUDA(dalloc(L.R.pend_node[k], chunks * kListChunk));
+            NG_CUDA(dalloc(L.R.pend_feat[k], chunks * kListChunk));
+            NG_CUDA(dalloc(L.R.pend_next[k], chunks));
+            NG_CUDA(dalloc(L.R.pend_owner[k], chunks));
+            NG_CUDA(dalloc(L.R.pend_fill[k], chunks));
+        }
+        dfree(L.R.dec);
+        NG_CUDA(dalloc(L.R.dec, chunks * kListChunk));
+        L.R.pend_chunk_cap = (int)chunks;
+    }
+    return NGRAV_OK;
+}
+
 }  // namespace
 
 void lmac_destroy(ngrav_gpu_ctx* ctx) {
@@ -249,13 +297,29 @@ void lmac_destroy(ngrav_gpu_ctx* ctx) {
     dfree(L.dModel); dfree(L.dP); dfree(L.dM); dfree(L.dV); dfree(L.dGrad); dfree(L.dPartial); dfree(L.dStats);
     dfree(L.dXb); dfree(L.dyb); dfree(L.dwb); dfree(L.dX); dfree(L.dR); dfree(L.dPairs); dfree(L.dCnt);
     dfree(L.dWork); dfree(L.dStatus); dfree(L.dZ);
+    free_rounds(L);
     delete ctx->lm;
     ctx->lm = nullptr;
 }
 
+bool lmac_prepare(ngrav_gpu_ctx* ctx) {
+    LmacState* L = ctx->lm;
+    bool use = ctx->opts.mac == NGRAV_MAC_LEARNED && L && L->have_model && !L->reverted && ctx->acc_valid;
+    if (use) {
+        // every group may park once per round; pools start at 64 deferred
+        // pairs per particle (grown to what a round needs if that is short)
+        const long long groups = std::max<long long>(ctx->cap_n, 1);
+        const long long est = ctx->n / 2 + 1024;
+        if (ensure_rounds(ctx, groups, std::max<long long>(L->R.pend_chunk_cap, est)) != NGRAV_OK) use = false;
+        L->R.rounds = std::max(2, std::min(kLmMaxRounds, L->opts.rounds));
+    }
+    if (L) L->prepared = use;
+    return use;
+}
+
 bool lmac_walk_setup(ngrav_gpu_ctx* ctx, WalkParams& wp, const void** model) {
     LmacState* L = ctx->lm;
-    const bool use = ctx->opts.mac == NGRAV_MAC_LEARNED && L && L->have_model && !L->reverted && ctx->acc_valid;
+    const bool use = L && L->prepared;
     if (L) L->used_last = use;
     if (!use) return false;
     wp.learned = 1;
@@ -263,12 +327,51 @@ bool lmac_walk_setup(ngrav_gpu_ctx* ctx, WalkParams& wp, const void** model) {
     wp.lm_gate = (float)L->opts.gate;
     wp.lm_rho_lo = (float)L->opts.rho_lo;
     wp.lm_rho_hi = (float)L->opts.rho_hi;
+    wp.lm_screen = (float)L->opts.screen;
+    wp.lm_budget = (float)L->opts.budget;
+    for (int i = 0; i < kLmacIn; ++i) {
+        wp.lm_mu[i] = L->norm.mu[i];
+        wp.lm_isd[i] = L->norm.isd[i];
+    }
     *model = L->dModel;
     return true;
 }
 
+void lmac_key(const ngrav_gpu_ctx* ctx, std::vector<unsigned char>& key) {
+    const LmacState* L = ctx->lm;
+    const unsigned char on = (L && L->prepared) ? 1 : 0;
+    key.push_back(on);
+    if (!on) return;
+    auto put = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + n);
+    };
+    put(&L->R, sizeof(L->R));
+    put(&L->dModel, sizeof(L->dModel));
+    put(&L->opts, sizeof(L->opts));
+    put(&L->norm, sizeof(L->norm));
+}
+
 void lmac_launch_walk(ngrav_gpu_ctx* ctx, const WalkParams& wp, const void* model) {
-    launch_walk_lmac(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, static_cast<const LmacDev*>(model), ctx->stream);
+    LmacState& L = *ctx->lm;
+    cudaStream_t s = ctx->stream;
+    cudaMemsetAsync(L.R.ctr, 0, sizeof(int) * 4 * kLmMaxRounds, s);
+    for (int r = 0; r < L.R.rounds; ++r) {
+        launch_walk_lmac_round(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, L.R, r, s);
+        if (r + 1 < L.R.rounds)
+            launch_lmac_infer(ctx->T, ctx->C, wp, L.R, r, static_cast<const LmacDev*>(model), ctx->sm_count, s);
+    }
+    ctx->launches += 2 * L.R.rounds - 2;  // beyond the one walk launch counted by the caller
+}
+
+int lmac_grow_pools(ngrav_gpu_ctx* ctx) {
+    LmacState& L = *ctx->lm;
+    int ctr[4 * kLmMaxRounds];
+    NG_CUDA(cudaMemcpy(ctr, L.R.ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
+    long long need = 0;
+    for (int r = 0; r < kLmMaxRounds; ++r) need = std::max<long long>(need, ctr[4 * r + 2]);
+    if (need >= 0x7FFFFFF0LL / kListChunk) return fail(ctx, NGRAV_ERR_CAPACITY, "deferred-pair pool exhausted");
+    return ensure_rounds(ctx, L.gs_cap, std::max<long long>(need + need / 4 + 1024, 2LL * L.R.pend_chunk_cap));
 }
 
 int lmac_after_eval(ngrav_gpu_ctx* ctx) {
@@ -294,6 +397,7 @@ void lmac_fill_stats(const ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->lmac_accepts = (long long)c.lm_accepts;
     out->lmac_fallbacks = (long long)c.lm_fallbacks;
     out->lmac_flushes = (long long)c.lm_flushes;
+    out->lmac_screened = (long long)c.lm_screened;
     const LmacState* L = ctx->lm;
     out->lmac_active = (L && ctx->opts.mac == NGRAV_MAC_LEARNED && L->have_model && !L->reverted) ? 1 : 0;
     out->lmac_reverted = (L && L->reverted) ? 1 : 0;
@@ -317,13 +421,16 @@ int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o) {
     o->check_every = 10;
     o->check_targets = 4096;
     o->revert_rms = 1e-3;
+    o->rounds = 3;
+    o->screen = 1.0;
     return NGRAV_OK;
 }
 
 int ngrav_gpu_lmac_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_lmac_opts* o) {
     if (!ctx || !o) return NGRAV_ERR_INVALID_ARG;
     if (!(o->budget > 0.0) || !(o->gate >= 0.0) || !(o->rho_lo >= 0.0) || !(o->rho_hi > o->rho_lo) ||
-        o->check_every < 0 || o->check_targets < 0)
+        !(o->screen >= 0.0) ||
+        o->check_every < 0 || o->check_targets < 0 || o->rounds < 2 || o->rounds > kLmMaxRounds)
         return fail(ctx, NGRAV_ERR_INVALID_ARG, "learned MAC options out of range");
     NG_CUDA(cudaSetDevice(ctx->opts.device));
     NG_TRY(ensure_state(ctx));

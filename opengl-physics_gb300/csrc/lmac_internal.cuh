@@ -21,6 +21,39 @@ struct LmacRecordParams {
     unsigned long long* ndropped;     // groups cut short (stack or visit limit)
 };
 
+// ---- round-based learned walk (walk_lmac.cu) ----
+// A group between rounds: its interaction lists so far and its deferred pairs.
+struct LmacGroupState {
+    int far_first, far_cur, far_pos, far_count;
+    int near_first, near_cur, near_pos, near_count;
+    int pend_first, pend_count;
+    int pad[2];
+};
+
+constexpr int kLmMaxRounds = 8;
+// Per round r: ctr[4r] walk scheduler, ctr[4r+1] groups deferred, ctr[4r+2]
+// pending chunks taken, ctr[4r+3] unused.
+struct LmacRounds {
+    int rounds;                        // rounds this evaluation runs (the last decides geometrically)
+    LmacGroupState* gs;                // per group index
+    int* active[2];                    // group indices with deferred pairs (ping-pong by round parity)
+    int* pend_node[2];                 // deferred node ids, chunks of kListChunk (ping-pong)
+    uint4* pend_feat[2];               // their standardised features, 8 x BF16 per entry
+    int* pend_next[2];                 // chunk links
+    int* pend_owner[2];                // chunk -> group leaf
+    int* pend_fill[2];                 // chunk -> entries used
+    unsigned char* dec;                // decisions for the pool being resolved (1 = accept)
+    int pend_chunk_cap;
+    int* ctr;                          // 4 * kLmMaxRounds counters, zeroed per evaluation
+};
+
+void launch_walk_lmac_round(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
+                            const ListBuffers& LB, const LmacRounds& R, int round, cudaStream_t s);
+void launch_lmac_infer(const NodeArrays& T, Counters* C, const WalkParams& wp, const LmacRounds& R, int round,
+                       const LmacDev* model, int sm_count, cudaStream_t s);
+void launch_lmac_tc_forward(const LmacDev* model, const float* X, int n, float* z, unsigned* status, int sm_count,
+                            cudaStream_t s);
+
 void launch_lmac_record(const NodeArrays& T, const Counters* C, const int* leaf_list, const LmacRecordParams& rp,
                         int blocks, cudaStream_t s);
 void launch_lmac_amin(const NodeArrays& T, const Counters* C, const int* leaf_list, const float4* acc,

@@ -1,143 +1,267 @@
-// walk_lmac.cu -- the grouped walk with the learned opening test (lmac.cuh).
+// walk_lmac.cu -- the grouped walk with the learned opening test (lmac.cuh),
+// run in rounds.
 //
 // Same traversal and list output as walk_kernel (walk.cu; semantics of the
 // reference's grouped walk, Solvers.cpp:248-355), with the opening decision of
 // an internal node replaced:
 //   worst <= 0 or 2h >= rho_hi * worst   -> open
 //   2h <= rho_lo * worst                 -> accept (far)
-//   otherwise                            -> ask the network
-// Pairs for the network wait in a per-warp queue of 64 slots whose features sit
-// in the CTA's shared operand tile; the four warps of a CTA advance in step and
-// the CTA evaluates all queued pairs with one tensor-core flush (lmac_tc.cuh)
-// whenever some warp's queue is full or some warp has nothing else to do.  A
-// flushed pair is accepted iff its logit z > gate, opened iff z < -gate, and
-// decided by the geometric test with the run's theta otherwise.
+//   otherwise                            -> the network decides
+// Round r of the walk (walk_lmac_round_kernel) resolves the group's deferred
+// pairs of round r-1 (accept -> far list, open -> children onto the stack),
+// then walks until its stack is empty, deferring every pair for the network
+// into a chunked per-group pending list.  Between rounds, lmac_infer_kernel
+// evaluates every deferred pair of the round on the tensor cores
+// (lmac_tc.cuh, 256 pairs per CTA flush) and stores the decision: accept iff
+// the logit z > gate, open iff z < -gate, the geometric test with the run's
+// theta otherwise.  The last round decides its band pairs geometrically, so
+// every group's lists are complete after it.  Traversal warps never wait for
+// the tensor cores, and the tensor-core kernel runs as a streaming batch.
 //
-// lmac_tc_forward_kernel evaluates the same routine on given features (the
-// unit test of the tensor-core path against the oracle).
+// lmac_tc_forward_kernel evaluates the same network routine on given features
+// (the unit test of the tensor-core path against the oracle).
 #include "engine.cuh"
 #include "lmac.cuh"
+#include "lmac_internal.cuh"
 #include "lmac_tc.cuh"
 #include "walk_common.cuh"
 
 namespace ngrav {
 
-constexpr int kLmWarps = 4;
-constexpr int kLmThreads = kLmWarps * 32;
-constexpr int kLmStack = 1024;  // per-warp shared-memory traversal stack
-constexpr int kLmQueue = 64;
+constexpr int kLwWarps = 4;
+constexpr int kLwThreads = kLwWarps * 32;
+constexpr int kLwStack = 2048;  // per-warp shared-memory traversal stack
 
-size_t walk_lmac_smem_bytes() {
-    return sizeof(LmacTiles) + 1024 + sizeof(int) * (kLmWarps * kLmQueue + 8 + kLmWarps * kLmStack);
+// Append to a group's deferred-pair list: chunks taken one at a time (so
+// every chunk counted is owned and filled), owner and fill recorded for the
+// tensor-core kernel.
+__device__ __forceinline__ void pend_append(ChunkList& L, bool has, int val, uint4 feat, const LmacRounds& R, int out,
+                                            int* counter, int leaf, int lane, unsigned lt_mask, unsigned& bad) {
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    const int k = __popc(m);
+    if (k == 0) return;
+    const int cap = R.pend_chunk_cap;
+    if (L.cur < 0) {
+        int c = 0;
+        if (lane == 0) {
+            c = atomicAdd(counter, 1);
+            if (c < cap) R.pend_owner[out][c] = leaf;
+        }
+        L.cur = L.first = __shfl_sync(0xffffffffu, c, 0);
+        L.pos = 0;
+    }
+    int newc = -1;
+    if (L.pos + k > kListChunk) {
+        if (lane == 0) {
+            newc = atomicAdd(counter, 1);
+            if (L.cur < cap) {
+                R.pend_next[out][L.cur] = newc;
+                R.pend_fill[out][L.cur] = kListChunk;
+            }
+            if (newc < cap) R.pend_owner[out][newc] = leaf;
+        }
+        newc = __shfl_sync(0xffffffffu, newc, 0);
+    }
+    if (has) {
+        const int i = L.pos + __popc(m & lt_mask);
+        const int c = i < kListChunk ? L.cur : newc;
+        const int p = i < kListChunk ? i : i - kListChunk;
+        if (c < cap) {
+            R.pend_node[out][(long long)c * kListChunk + p] = val;
+            R.pend_feat[out][(long long)c * kListChunk + p] = feat;
+        } else {
+            bad |= kStPendOverflow;
+        }
+    }
+    if (newc >= 0) {
+        L.cur = newc;
+        L.pos = L.pos + k - kListChunk;
+    } else {
+        L.pos += k;
+    }
+    L.count += k;
+}
+
+// Standardised features as the tensor-core operand row: 8 x BF16.
+__device__ __forceinline__ uint4 lmac_row(const float f[kLmacIn], const WalkParams& wp) {
+    uint4 v;
+    v.x = pack_bf16x2((f[0] - wp.lm_mu[0]) * wp.lm_isd[0], (f[1] - wp.lm_mu[1]) * wp.lm_isd[1]);
+    v.y = pack_bf16x2((f[2] - wp.lm_mu[2]) * wp.lm_isd[2], (f[3] - wp.lm_mu[3]) * wp.lm_isd[3]);
+    v.z = pack_bf16x2((f[4] - wp.lm_mu[4]) * wp.lm_isd[4], (f[5] - wp.lm_mu[5]) * wp.lm_isd[5]);
+    v.w = pack_bf16x2((f[6] - wp.lm_mu[6]) * wp.lm_isd[6], (f[7] - wp.lm_mu[7]) * wp.lm_isd[7]);
+    return v;
+}
+
+__device__ __forceinline__ bool geometric_accept(const float4 A, const float4 Cw, const float4 D, const float4 gA,
+                                                 const float4 gD, float gR, float theta2) {
+    const float dx = (A.x - gA.x) + (D.x - gD.x);
+    const float dy = (A.y - gA.y) + (D.y - gD.y);
+    const float dz = (A.z - gA.z) + (D.z - gD.z);
+    const float worst = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - gR;
+    return worst > 0.f && Cw.y * Cw.y < theta2 * worst * worst;
 }
 
 template <bool SMEM_STACK>
-__global__ void __launch_bounds__(kLmThreads) walk_lmac_kernel(NodeArrays T, Counters* C,
-                                                               const int* __restrict__ leaf_list, WalkParams wp,
-                                                               ListBuffers LB, const LmacDev* __restrict__ model) {
-    extern __shared__ unsigned char lm_dyn[];
-    LmacTiles& S = *lmac_tiles_at(lm_dyn);
-    int* pend_all = reinterpret_cast<int*>(&S + 1);
-    int* flags = pend_all + kLmWarps * kLmQueue;
-    int* s_stack = flags + 8;
+__global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArrays T, Counters* C,
+                                                                     const int* __restrict__ leaf_list,
+                                                                     WalkParams wp, ListBuffers LB, LmacRounds R,
+                                                                     int round) {
+    __shared__ int s_stack[SMEM_STACK ? kLwWarps * kLwStack : 1];
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int gwarp = blockIdx.x * kLmWarps + warp;
-    lmac_tc_init(S, model);
-    int* pend = pend_all + warp * kLmQueue;
-    int* stack = SMEM_STACK ? s_stack + warp * kLmStack : LB.stack + (long long)gwarp * LB.stack_cap;
-    const int stack_cap = SMEM_STACK ? kLmStack : LB.stack_cap;
-    const int nleaves = C->nleaves;
+    const int gwarp = blockIdx.x * kLwWarps + (threadIdx.x >> 5);
+    if (C->status & kStFatal) return;
+    int* stack = SMEM_STACK ? s_stack + (threadIdx.x >> 5) * kLwStack : LB.stack + (long long)gwarp * LB.stack_cap;
+    const int stack_cap = SMEM_STACK ? kLwStack : LB.stack_cap;
+    const bool last = round == R.rounds - 1;
+    const int in = (round + 1) & 1, out = round & 1;
+    const int ngroups = round == 0 ? C->nleaves : R.ctr[4 * (round - 1) + 1];
+    int* sched = R.ctr + 4 * round;
+    int* active_out = R.active[out];
+    int* pend_ctr = R.ctr + 4 * round + 2;
     const unsigned lt_mask = (1u << lane) - 1u;
     const float eps = sqrtf(wp.eps2);
-    unsigned long long tests = 0, groups = 0, queries = 0, accepts = 0, fallbacks = 0, flushes = 0;
+    unsigned long long tests = 0, groups = 0, resolved = 0, screened = 0;
     int stack_max = 0, list_max = 0;
     unsigned bad = 0;
     int fres_next = 0, fres_end = 0, nres_next = 0, nres_end = 0;
-    bool active = false, exhausted = (C->status & kStFatal) != 0;
-    int gi = 0, leaf = 0, size = 0, npend = 0, visits = 0;
-    float4 gA = make_float4(0.f, 0.f, 0.f, 0.f), gD = gA;
-    float gR = 0.f, amin = 0.f;
-    ChunkList far = {-1, -1, 0, 0, 0, 0}, near = far;
-    uint32_t phase = 0;
-    int it = 0;
 
     for (;;) {
-        // ---- take a new group ----
-        if (!active && !exhausted) {
-            int g = 0;
-            if (lane == 0) g = atomicAdd(&C->work_next, 1);
-            g = __shfl_sync(0xffffffffu, g, 0);
-            if (g >= nleaves) {
-                exhausted = true;
-            } else {
-                gi = g;
-                leaf = leaf_list[gi];
-                gA = T.wA[leaf];
-                gD = T.wD[leaf];
-                gR = T.wC[leaf].x;
-                amin = T.amin[leaf];
-                ++groups;
-                far = {-1, -1, 0, 0, fres_next, fres_end};
-                near = {-1, -1, 0, 0, nres_next, nres_end};
-                list_append(near, lane == 0, leaf, LB.near, LB.near_next, &C->near_chunks, LB.near_chunk_cap,
-                            lane, lt_mask, bad);
-                size = 0;
-                if (leaf != 0) {
-                    if (lane == 0) stack[0] = 0;
-                    size = 1;
-                }
-                visits = 0;
-                npend = 0;
-                active = true;
-                __syncwarp();
+        int k = 0;
+        if (lane == 0) k = atomicAdd(sched, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= ngroups) break;
+        const int gi = round == 0 ? k : R.active[in][k];
+        const int leaf = leaf_list[gi];
+        const float4 gA = T.wA[leaf];
+        const float4 gD = T.wD[leaf];
+        const float gR = T.wC[leaf].x;
+        const float amin = T.amin[leaf];
+        ChunkList far, near, pend = {-1, -1, 0, 0, 0, 0};
+        int size = 0;
+        if (round == 0) {
+            ++groups;
+            far = {-1, -1, 0, 0, fres_next, fres_end};
+            near = {-1, -1, 0, 0, nres_next, nres_end};
+            list_append(near, lane == 0, leaf, LB.near, LB.near_next, &C->near_chunks, LB.near_chunk_cap, lane,
+                        lt_mask, bad);
+            if (leaf != 0) {
+                if (lane == 0) stack[0] = 0;
+                size = 1;
             }
+        } else {
+            const LmacGroupState g = R.gs[gi];
+            far = {g.far_first, g.far_cur, g.far_pos, g.far_count, fres_next, fres_end};
+            near = {g.near_first, g.near_cur, g.near_pos, g.near_count, nres_next, nres_end};
+            // resolve the deferred pairs of the previous round, 32 at a time
+            int chunk = g.pend_first;
+            for (int i0 = 0; i0 < g.pend_count; i0 += 32) {
+                const int e = (i0 & (kListChunk - 1)) + lane;
+                const bool has = i0 + lane < g.pend_count;
+                int node = -1, nch = 0, link = 0;
+                bool acc = false;
+                if (has) {
+                    const long long slot = (long long)chunk * kListChunk + e;
+                    node = R.pend_node[in][slot];
+                    acc = R.dec[slot] != 0;
+                    if (!acc) {
+                        const float4 Cw = T.wC[node];
+                        nch = __float_as_int(Cw.w) & 0xFFFFFF;
+                        link = __float_as_int(Cw.z);
+                    }
+                }
+                resolved += __popc(__ballot_sync(0xffffffffu, has));
+                list_append(far, has && acc, node, LB.far, LB.far_next, &C->far_chunks, LB.far_chunk_cap, lane,
+                            lt_mask, bad);
+                int tot;
+                const int off = warp_excl_scan(nch, lane, tot);
+                if (size + tot > stack_cap) {
+                    bad |= kStStackOverflow;
+                    break;
+                }
+                for (int q = 0; q < nch; ++q) stack[size + off + q] = link + q;
+                size += tot;
+                if (((i0 + 32) & (kListChunk - 1)) == 0 && i0 + 32 < g.pend_count) chunk = R.pend_next[in][chunk];
+            }
+            __syncwarp();
         }
-        // ---- one traversal step: up to 64 nodes, as the queue allows ----
-        if (active && size > 0 && npend < kLmQueue) {
-            const int take = min(size, kLmQueue - npend);
+        int visits = 0;
+        while (size > 0 && !(bad & (kStStackOverflow | kStCorrupt))) {
+            const int take = min(size, 64);
             size -= take;
             visits += take;
+            if (visits > wp.node_limit) {
+                bad |= kStCorrupt;
+                break;
+            }
             int node[2];
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 const int idx = lane + 32 * q;
                 node[q] = idx < take ? stack[size + idx] : -1;
             }
+            float4 A[2], Cw[2], D[2], B[2];
+            int cnt[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {  // every record in flight at once
+                if (node[q] >= 0) {
+                    A[q] = T.wA[node[q]];
+                    Cw[q] = T.wC[node[q]];
+                    D[q] = T.wD[node[q]];
+                    B[q] = T.wB[node[q]];
+                    cnt[q] = T.count[node[q]];
+                } else {
+                    A[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    Cw[q] = A[q];
+                    D[q] = A[q];
+                    B[q] = A[q];
+                    cnt[q] = 0;
+                }
+            }
             __syncwarp();
             int kind[2], nch[2], link[2];
-            float feat[2][kLmacIn];
+            uint4 row[2];
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
-                kind[q] = 0;  // 0 none, 1 near, 2 far, 3 open, 4 ask the network
+                kind[q] = 0;  // 0 none, 1 near, 2 far, 3 open, 4 deferred
                 nch[q] = 0;
-                link[q] = 0;
-                const int nd = node[q];
-                if (nd >= 0 && nd != leaf) {
-                    const float4 A = T.wA[nd];
-                    const float4 Cw = T.wC[nd];
-                    const int meta = __float_as_int(Cw.w);
-                    link[q] = __float_as_int(Cw.z);
-                    if (A.w > 0.f) {
-                        if (meta < 0) {
-                            kind[q] = 1;
-                        } else {
-                            const float4 D = T.wD[nd];
-                            const float dx = (A.x - gA.x) + (D.x - gD.x);
-                            const float dy = (A.y - gA.y) + (D.y - gD.y);
-                            const float dz = (A.z - gA.z) + (D.z - gD.z);
-                            const float worst = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - gR;
-                            const float sz = Cw.y;
-                            if (!(worst > 0.f) || sz >= wp.lm_rho_hi * worst) {
-                                kind[q] = 3;
-                            } else if (sz <= wp.lm_rho_lo * worst) {
-                                kind[q] = 2;
-                            } else {
-                                kind[q] = 4;
-                                lmac_features(gA, gD, gR, amin, A, T.wB[nd], Cw, D, T.count[nd], wp.G, eps,
-                                              wp.lm_log2b, feat[q]);
+                row[q] = make_uint4(0u, 0u, 0u, 0u);
+                link[q] = __float_as_int(Cw[q].z);
+                const int meta = __float_as_int(Cw[q].w);
+                if (node[q] >= 0 && node[q] != leaf && A[q].w > 0.f) {
+                    if (meta < 0) {
+                        kind[q] = 1;
+                    } else {
+                        const float dx = (A[q].x - gA.x) + (D[q].x - gD.x);
+                        const float dy = (A[q].y - gA.y) + (D[q].y - gD.y);
+                        const float dz = (A[q].z - gA.z) + (D[q].z - gD.z);
+                        const float worst = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - gR;
+                        const float sz = Cw[q].y;
+                        if (!(worst > 0.f) || sz >= wp.lm_rho_hi * worst) {
+                            kind[q] = 3;
+                        } else if (sz <= wp.lm_rho_lo * worst) {
+                            kind[q] = 2;
+                        } else if (!last) {
+                            kind[q] = 4;
+                            // Quadrupole truncation bound on every member (Salmon & Warren
+                            // 1994, p = 2): |da| <= G M / w^2 * 4 x^3 / (1 - x)^2, x = maxR / w.
+                            const float x = Cw[q].x / worst;
+                            if (wp.lm_screen > 0.f && x < 1.f) {
+                                const float om = 1.f - x;
+                                const float bound = wp.G * A[q].w / (worst * worst) * 4.f * x * x * x / (om * om);
+                                if (bound <= wp.lm_screen * wp.lm_budget * amin) {
+                                    kind[q] = 2;
+                                    ++screened;
+                                }
                             }
-                            if (kind[q] == 3) nch[q] = meta & 0xFFFFFF;
+                        } else {
+                            kind[q] = sz * sz < wp.theta2 * worst * worst ? 2 : 3;
+                        }
+                        if (kind[q] == 3) nch[q] = meta & 0xFFFFFF;
+                        if (kind[q] == 4) {
+                            float f[kLmacIn];
+                            lmac_features(gA, gD, gR, amin, A[q], B[q], Cw[q], D[q], cnt[q], wp.G, eps, wp.lm_log2b,
+                                          f);
+                            row[q] = lmac_row(f, wp);
                         }
                     }
                 }
@@ -149,13 +273,7 @@ __global__ void __launch_bounds__(kLmThreads) walk_lmac_kernel(NodeArrays T, Cou
                             LB.near_chunk_cap, lane, lt_mask, bad);
                 list_append(far, kind[q] == 2, node[q], LB.far, LB.far_next, &C->far_chunks, LB.far_chunk_cap,
                             lane, lt_mask, bad);
-                const unsigned m = __ballot_sync(0xffffffffu, kind[q] == 4);
-                if (kind[q] == 4) {
-                    const int slot = npend + __popc(m & lt_mask);
-                    lmac_put_features(S, warp, slot, feat[q]);
-                    pend[slot] = node[q];
-                }
-                npend += __popc(m);
+                pend_append(pend, kind[q] == 4, node[q], row[q], R, out, pend_ctr, leaf, lane, lt_mask, bad);
             }
             bool ovf = false;
 #pragma unroll
@@ -166,133 +284,148 @@ __global__ void __launch_bounds__(kLmThreads) walk_lmac_kernel(NodeArrays T, Cou
                     ovf = true;
                     break;
                 }
-                for (int k = 0; k < nch[q]; ++k) stack[size + off + k] = link[q] + k;
+                for (int c = 0; c < nch[q]; ++c) stack[size + off + c] = link[q] + c;
                 size += tot;
             }
-            if (ovf || visits > wp.node_limit) {
-                bad |= ovf ? kStStackOverflow : kStCorrupt;
-                active = false;  // the host re-runs the evaluation (larger stack) or reports
-                exhausted = true;
-                npend = 0;
-            }
+            if (ovf) bad |= kStStackOverflow;
             stack_max = max(stack_max, size);
             __syncwarp();
         }
-        // ---- CTA step: flush when some warp needs the network ----
-        const bool need = active && npend > 0 && (npend == kLmQueue || size == 0);
-        const bool done = exhausted && !active;
-        if (lane == 0) flags[(it & 1) * 4 + warp] = (need ? 1 : 0) | (done ? 2 : 0);
-        __syncthreads();
-        int any_need = 0, all_done = 2;
-#pragma unroll
-        for (int w = 0; w < kLmWarps; ++w) {
-            const int f = flags[(it & 1) * 4 + w];
-            any_need |= f & 1;
-            all_done &= f & 2;
-        }
-        ++it;
-        if (all_done) break;
-        if (any_need) {
-            float z0 = 0.f, z1 = 0.f;
-            const bool ok = lmac_tc_flush(S, warp, lane, phase, z0, z1);
-            ++flushes;
-            if (!ok) {
-                bad |= kStTimeout;
-                active = false;
-                exhausted = true;
-                npend = 0;
+        fres_next = far.res_next;
+        fres_end = far.res_end;
+        nres_next = near.res_next;
+        nres_end = near.res_end;
+        if (pend.count > 0) {
+            // park the group until the network has decided its pairs
+            if (lane == 0) {
+                if (pend.cur < R.pend_chunk_cap) R.pend_fill[out][pend.cur] = pend.pos;
+                LmacGroupState g;
+                g.far_first = far.first;
+                g.far_cur = far.cur;
+                g.far_pos = far.pos;
+                g.far_count = far.count;
+                g.near_first = near.first;
+                g.near_cur = near.cur;
+                g.near_pos = near.pos;
+                g.near_count = near.count;
+                g.pend_first = pend.first;
+                g.pend_count = pend.count;
+                g.pad[0] = g.pad[1] = 0;
+                R.gs[gi] = g;
+                active_out[atomicAdd(R.ctr + 4 * round + 1, 1)] = gi;
             }
-            if (npend > 0) {
-                int kind[2], nch[2], link[2], node[2];
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const int slot = lane + 32 * q;
-                    node[q] = slot < npend ? pend[slot] : -1;
-                    kind[q] = 0;
-                    nch[q] = 0;
-                    link[q] = 0;
-                    if (node[q] >= 0) {
-                        const float z = q ? z1 : z0;
-                        const float4 Cw = T.wC[node[q]];
-                        bool acc;
-                        if (fabsf(z) >= wp.lm_gate) {
-                            acc = z > 0.f;
-                        } else {  // low confidence: the geometric test decides
-                            const float4 A = T.wA[node[q]], D = T.wD[node[q]];
-                            const float dx = (A.x - gA.x) + (D.x - gD.x);
-                            const float dy = (A.y - gA.y) + (D.y - gD.y);
-                            const float dz = (A.z - gA.z) + (D.z - gD.z);
-                            const float worst = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - gR;
-                            acc = worst > 0.f && Cw.y * Cw.y < wp.theta2 * worst * worst;
-                            ++fallbacks;
-                        }
-                        kind[q] = acc ? 2 : 3;
-                        if (acc) ++accepts;
-                        if (!acc) {
-                            nch[q] = __float_as_int(Cw.w) & 0xFFFFFF;
-                            link[q] = __float_as_int(Cw.z);
-                        }
-                    }
-                }
-                queries += npend;
-                bool ovf = false;
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    list_append(far, kind[q] == 2, node[q], LB.far, LB.far_next, &C->far_chunks,
-                                LB.far_chunk_cap, lane, lt_mask, bad);
-                    int tot;
-                    const int off = warp_excl_scan(nch[q], lane, tot);
-                    if (size + tot > stack_cap) {
-                        ovf = true;
-                        break;
-                    }
-                    for (int k = 0; k < nch[q]; ++k) stack[size + off + k] = link[q] + k;
-                    size += tot;
-                }
-                npend = 0;
-                if (ovf) {
-                    bad |= kStStackOverflow;
-                    active = false;
-                    exhausted = true;
-                }
-                stack_max = max(stack_max, size);
-                __syncwarp();
-            }
-        }
-        // ---- group finished ----
-        if (active && size == 0 && npend == 0) {
-            fres_next = far.res_next;
-            fres_end = far.res_end;
-            nres_next = near.res_next;
-            nres_end = near.res_end;
+        } else {
             if (lane == 0) LB.ginfo[gi] = make_int4(far.first, near.first, far.count, near.count);
             list_max = max(list_max, max(far.count, near.count));
-            active = false;
         }
+        if (bad & (kStStackOverflow | kStCorrupt)) break;
     }
-    lmac_tc_release(S);
     for (int o = 16; o > 0; o >>= 1) {
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-        fallbacks += __shfl_xor_sync(0xffffffffu, fallbacks, o);
-        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        screened += __shfl_xor_sync(0xffffffffu, screened, o);
     }
     if (lane == 0) {
         if (bad) atomicOr(&C->status, bad);
         atomicAdd(&C->mac_tests, tests);
-        atomicAdd(&C->groups, groups);
-        atomicAdd(&C->lm_queries, queries);
-        atomicAdd(&C->lm_accepts, accepts);
-        atomicAdd(&C->lm_fallbacks, fallbacks);
+        if (screened) atomicAdd(&C->lm_screened, screened);
+        if (groups) atomicAdd(&C->groups, groups);
         atomicMax(&C->stack_max, stack_max);
         atomicMax(&C->list_max, list_max);
     }
-    if (threadIdx.x == 0) atomicAdd(&C->lm_flushes, flushes);
+    (void)resolved;
+}
+
+// Decide every deferred pair of `round`: pairs of chunks 2t and 2t+1 form
+// tile t (entry e of chunk 2t+h is pair slot 32h + (e % 32) of warp e / 32).
+// The walk stored each pair's operand row; a CTA streams its tiles, loading
+// the next tile's rows while the current one is on the tensor cores.
+__global__ void __launch_bounds__(kLwThreads) lmac_infer_kernel(NodeArrays T, Counters* C, WalkParams wp,
+                                                                LmacRounds R, int round,
+                                                                const LmacDev* __restrict__ model) {
+    extern __shared__ unsigned char lm_dyn[];
+    LmacTiles& S = *lmac_tiles_at(lm_dyn);
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int e = threadIdx.x;  // entry within a chunk
+    __shared__ unsigned s_status;
+    if (threadIdx.x == 0) s_status = C->status;
+    __syncthreads();
+    if (s_status & kStFatal) return;  // uniform across the CTA
+    const int pool = round & 1;
+    int nchunks = R.ctr[4 * round + 2];
+    nchunks = nchunks < R.pend_chunk_cap ? nchunks : R.pend_chunk_cap;
+    const int ntiles = (nchunks + 1) / 2;
+    if ((int)blockIdx.x >= ntiles) return;
+    lmac_tc_init(S, model);
+    const uint4* feat = R.pend_feat[pool];
+    const int* fill = R.pend_fill[pool];
+    unsigned char* a1 = reinterpret_cast<unsigned char*>(S.a2);
+    uint32_t phase = 0;
+    bool ok_all = true;
+    unsigned long long queries = 0, accepts = 0, fallbacks = 0, flushes = 0;
+    // Rows are loaded without waiting for the fill counts (slots past a
+    // chunk's fill hold stale rows whose logits are never used).
+    auto load_tile = [&](int t, uint4 rows[2], int fills[2]) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = 2 * t + h;
+            const bool in = c < nchunks;
+            fills[h] = in ? fill[c] : 0;
+            rows[h] = in ? feat[(long long)c * kListChunk + e] : make_uint4(0u, 0u, 0u, 0u);
+        }
+    };
+    uint4 rows[2];
+    int fills[2];
+    int t = blockIdx.x;
+    load_tile(t, rows, fills);
+    for (; t < ntiles; t += gridDim.x) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            *reinterpret_cast<uint4*>(a1 + tc::kmajor_offset(32 * warp + lane, 8 * h, kA1Lbo, kA1Sbo)) = rows[h];
+        const bool cur_valid[2] = {e < fills[0], e < fills[1]};
+        if (t + (int)gridDim.x < ntiles) load_tile(t + gridDim.x, rows, fills);  // in flight during the MMAs
+        float z[2];
+        ok_all = lmac_tc_flush(S, warp, lane, phase, z[0], z[1]) && ok_all;
+        ++flushes;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!cur_valid[h]) continue;
+            const long long slot = (long long)(2 * t + h) * kListChunk + e;
+            bool acc;
+            if (fabsf(z[h]) >= wp.lm_gate) {
+                acc = z[h] > 0.f;
+            } else {  // low confidence: the geometric test decides
+                const int nd = R.pend_node[pool][slot];
+                const int leaf = R.pend_owner[pool][2 * t + h];
+                acc = geometric_accept(T.wA[nd], T.wC[nd], T.wD[nd], T.wA[leaf], T.wD[leaf], T.wC[leaf].x, wp.theta2);
+                ++fallbacks;
+            }
+            ++queries;
+            if (acc) ++accepts;
+            R.dec[slot] = acc ? 1 : 0;
+        }
+    }
+    lmac_tc_release(S);
+    for (int o = 16; o > 0; o >>= 1) {
+        queries += __shfl_xor_sync(0xffffffffu, queries, o);
+        accepts += __shfl_xor_sync(0xffffffffu, accepts, o);
+        fallbacks += __shfl_xor_sync(0xffffffffu, fallbacks, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&C->lm_queries, queries);
+        atomicAdd(&C->lm_accepts, accepts);
+        atomicAdd(&C->lm_fallbacks, fallbacks);
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(&C->lm_flushes, flushes);
+        if (!ok_all) atomicOr(&C->status, kStTimeout);
+    }
 }
 
 // Logits of n pairs from raw features X[n][8] (standardised with the model's
 // statistics inside), 256 pairs per CTA flush: pair base + 64 w + p sits in
 // slot p of warp w.  status |= kStTimeout if a wait ran out.
-__global__ void __launch_bounds__(kLmThreads) lmac_tc_forward_kernel(const LmacDev* __restrict__ model,
+__global__ void __launch_bounds__(kLwThreads) lmac_tc_forward_kernel(const LmacDev* __restrict__ model,
                                                                      const float* __restrict__ X, int n,
                                                                      float* __restrict__ z,
                                                                      unsigned* __restrict__ status) {
@@ -322,44 +455,39 @@ __global__ void __launch_bounds__(kLmThreads) lmac_tc_forward_kernel(const LmacD
     if (!ok_all) atomicOr(status, kStTimeout);
 }
 
-void launch_walk_lmac(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
-                      const ListBuffers& LB, const LmacDev* model, cudaStream_t s) {
-    const size_t smem = walk_lmac_smem_bytes();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(walk_lmac_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(walk_lmac_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
-    const int blocks = (LB.nwarps + kLmWarps - 1) / kLmWarps;
-    if (wp.global_stack)
-        walk_lmac_kernel<false><<<blocks, kLmThreads, smem, s>>>(T, C, leaf_list, wp, LB, model);
-    else
-        walk_lmac_kernel<true><<<blocks, kLmThreads, smem, s>>>(T, C, leaf_list, wp, LB, model);
+static size_t tc_smem_bytes() { return sizeof(LmacTiles) + 1024; }
+
+// Dynamic shared-memory limits of the tensor-core kernels, set once at
+// context creation (never inside a graph capture).
+void lmac_set_attributes() {
+    const int smem = (int)tc_smem_bytes();
+    cudaFuncSetAttribute(lmac_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(lmac_tc_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
-int walk_lmac_blocks_per_sm() {
-    const size_t smem = walk_lmac_smem_bytes();
-    cudaFuncSetAttribute(walk_lmac_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, walk_lmac_kernel<true>, kLmThreads, smem);
-    // 64 tensor-memory columns per CTA: at most 8 CTAs share an SM's 512.
-    nb = nb < 8 ? nb : 8;
-    return nb > 0 ? nb : 1;
+void launch_walk_lmac_round(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
+                            const ListBuffers& LB, const LmacRounds& R, int round, cudaStream_t s) {
+    const int blocks = (LB.nwarps + kLwWarps - 1) / kLwWarps;
+    if (wp.global_stack)
+        walk_lmac_round_kernel<false><<<blocks, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+    else
+        walk_lmac_round_kernel<true><<<blocks, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+}
+
+void launch_lmac_infer(const NodeArrays& T, Counters* C, const WalkParams& wp, const LmacRounds& R, int round,
+                       const LmacDev* model, int sm_count, cudaStream_t s) {
+    const size_t smem = tc_smem_bytes();
+    // 64 tensor-memory columns per CTA: up to 8 CTAs per SM.
+    lmac_infer_kernel<<<sm_count * 7, kLwThreads, smem, s>>>(T, C, wp, R, round, model);
 }
 
 void launch_lmac_tc_forward(const LmacDev* model, const float* X, int n, float* z, unsigned* status, int sm_count,
                             cudaStream_t s) {
     if (n <= 0) return;
-    const size_t smem = walk_lmac_smem_bytes();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(lmac_tc_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
+    const size_t smem = tc_smem_bytes();
     long long blocks = ((long long)n + 255) / 256;
     if (blocks > (long long)sm_count * 4) blocks = (long long)sm_count * 4;
-    lmac_tc_forward_kernel<<<(unsigned)blocks, kLmThreads, smem, s>>>(model, X, n, z, status);
+    lmac_tc_forward_kernel<<<(unsigned)blocks, kLwThreads, smem, s>>>(model, X, n, z, status);
 }
 
 }  // namespace ngrav

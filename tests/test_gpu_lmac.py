@@ -129,7 +129,7 @@ def test_silenced_network_reproduces_geometric_walk(pkg, ic):
     sim.lmac_set_model(P, norm)
     # rho_lo below theta, rho_hi above: outside the band both tests agree;
     # inside it the gate silences the network, so the geometric test decides.
-    sim.lmac_set_opts(gate=1e30, rho_lo=0.25, rho_hi=1.25, check_every=0)
+    sim.lmac_set_opts(gate=1e30, rho_lo=0.25, rho_hi=1.25, check_every=0, screen=0.0)
     sim.set_opts(mac=pkg.MAC_LEARNED)
     a_lm = sim.compute_accel()
     s_lm = sim.stats()
@@ -166,4 +166,25 @@ def test_training_and_learned_walk(pkg, ic):
     sim.lmac_reset()
     sim.compute_accel()
     assert sim.stats()["lmac_queries"] > 0
+    sim.close()
+
+
+def test_error_bound_screen_is_safe(pkg, ic):
+    """Pairs the quadrupole truncation bound accepts without the network meet
+    the budget: with a budget so small that the network opens nearly
+    everything, screening only removes queries, it does not add error."""
+    n = 65536
+    sim, _ = plummer_system(pkg, ic, n, ncrit=16, theta=0.5)
+    sim.lmac_train(snapshots=2, steps_between=0, pairs=1 << 16, epochs=2, batch=4096, seed=2)
+    sim.set_opts(mac=pkg.MAC_LEARNED)
+    out = {}
+    for screen in (0.0, 1.0):
+        sim.lmac_set_opts(budget=1e-4, check_every=0, screen=screen)
+        sim.compute_accel()
+        st = sim.stats()
+        out[screen] = (st, sim.force_error(2048, seed=3, fp64_pairs=True))
+    assert out[0.0][0]["lmac_screened"] == 0
+    assert out[1.0][0]["lmac_screened"] > 0
+    assert out[1.0][0]["lmac_queries"] < out[0.0][0]["lmac_queries"]
+    assert out[1.0][1]["rms"] <= 1.2 * out[0.0][1]["rms"] + 1e-6
     sim.close()
