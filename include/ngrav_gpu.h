@@ -237,6 +237,53 @@ int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const f
  *   count          particles under each node; is_leaf
  *   center[3*nn], half, com[3*nn], mass, max_radius, quad[5*nn] (Qxx Qyy Qxy Qxz Qyz)
  * Node numbering is the GPU's own; compare in (level, prefix) order. */
+/* ---- autotuner ------------------------------------------------------------
+ * No reference counterpart.  Times force evaluations of the current state
+ * over candidate leaf capacities (= target-group sizes: every leaf is one
+ * group), P2P batch tiles (sources staged per near batch) and walk stack
+ * depths (per-warp shared-memory entries), keeps the fastest candidate whose
+ * rms force error (FP64-summed direct sum on check_targets samples) stays
+ * within rms_tolerance x that of the starting configuration, and installs
+ * it.  The state is not advanced. */
+typedef struct ngrav_gpu_tune_opts {
+    int reps;                  /* timed evaluations per candidate */
+    int check_targets;         /* targets of each error check */
+    double rms_tolerance;      /* admissible rms error / starting rms error */
+    int leaf_capacities[8];    /* candidates, 0-terminated; all 0: 8, 12, 16, 24, 32, 48 */
+} ngrav_gpu_tune_opts;
+
+typedef struct ngrav_gpu_tune_report {
+    int leaf_capacity, p2p_tile, walk_stack;   /* chosen */
+    double ms_before, ms_after;                /* force evaluation, device time */
+    double rms_before, rms_after;
+    int ntried;
+    double tried[32][5];                       /* leaf capacity, tile, stack, ms, rms (-1: not checked) */
+} ngrav_gpu_tune_report;
+
+int ngrav_gpu_default_tune_opts(ngrav_gpu_tune_opts* o);
+int ngrav_gpu_autotune(ngrav_gpu_ctx* ctx, const ngrav_gpu_tune_opts* o, ngrav_gpu_tune_report* out);
+/* Set the tuned kernel shapes directly: p2p_tile in {64, 128, 256} (0: 256),
+ * walk_stack in {1024, 2048, 4096}. */
+int ngrav_gpu_set_tuning(ngrav_gpu_ctx* ctx, int p2p_tile, int walk_stack);
+
+/* ---- ensembles of independent systems ------------------------------------
+ * No reference counterpart (the reference runs one System<3> per process).
+ * After ngrav_gpu_set_particles with the particles of nsys systems stored one
+ * system after another, system s occupying [offsets[s], offsets[s+1]), every
+ * system gets its own root cube and tree (System<3> semantics per system:
+ * no force between systems) and all systems advance together, one launch
+ * per phase.  nsys = 1 (or a new set_particles) returns to one system.
+ * Systems share G, eps, theta, leaf capacity and dt. */
+int ngrav_gpu_set_ensemble(ngrav_gpu_ctx* ctx, int nsys, const int64_t* offsets);
+/* rms[s] / max[s]: relative force error of system s against the direct sum
+ * over its own particles (FP32 pairs, FP64 sums) on targets_per_system
+ * sampled members. */
+int ngrav_gpu_ensemble_force_error(ngrav_gpu_ctx* ctx, int targets_per_system, uint64_t seed, double* rms,
+                                   double* max);
+/* FP64 diagnostics per system (out[nsys]); the potential is the exact pair
+ * sum when exact_potential, NaN otherwise. */
+int ngrav_gpu_ensemble_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_diag* out);
+
 /* ---- learned opening test (NGRAV_MAC_LEARNED) --------------------------
  * No reference counterpart: it replaces the geometric test of
  * include/ngrav/Mac.hpp:25-29 / src/Solvers.cpp:261-271 inside the grouped

@@ -42,6 +42,8 @@ EXPORTS = (
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
+    "ngrav_gpu_set_ensemble", "ngrav_gpu_ensemble_force_error", "ngrav_gpu_ensemble_diagnostics",
+    "ngrav_gpu_default_tune_opts", "ngrav_gpu_autotune", "ngrav_gpu_set_tuning",
     "ngrav_gpu_lmac_default_opts", "ngrav_gpu_lmac_set_opts", "ngrav_gpu_lmac_default_train_opts",
     "ngrav_gpu_lmac_train", "ngrav_gpu_lmac_get_model", "ngrav_gpu_lmac_set_model", "ngrav_gpu_lmac_reset",
     "ngrav_gpu_lmac_collect", "ngrav_gpu_lmac_forward", "ngrav_gpu_lmac_forward_tc", "ngrav_gpu_lmac_grad",
@@ -93,6 +95,17 @@ class Stats(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TuneOpts(ctypes.Structure):
+    _fields_ = [("reps", ctypes.c_int), ("check_targets", ctypes.c_int), ("rms_tolerance", ctypes.c_double),
+                ("leaf_capacities", ctypes.c_int * 8)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("leaf_capacity", ctypes.c_int), ("p2p_tile", ctypes.c_int), ("walk_stack", ctypes.c_int),
+                ("ms_before", ctypes.c_double), ("ms_after", ctypes.c_double), ("rms_before", ctypes.c_double),
+                ("rms_after", ctypes.c_double), ("ntried", ctypes.c_int), ("tried", (ctypes.c_double * 5) * 32)]
 
 
 class LmacOpts(ctypes.Structure):
@@ -179,6 +192,12 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_probe_fp32_peak.argtypes = [ctypes.c_int, _D]
     L.ngrav_gpu_diagnostics_noalloc.argtypes = [ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 7 + \
         [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Diag)]
+    L.ngrav_gpu_default_tune_opts.argtypes = [ctypes.POINTER(TuneOpts)]
+    L.ngrav_gpu_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(TuneOpts), ctypes.POINTER(TuneReport)]
+    L.ngrav_gpu_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    L.ngrav_gpu_set_ensemble.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+    L.ngrav_gpu_ensemble_force_error.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, _D, _D]
+    L.ngrav_gpu_ensemble_diagnostics.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Diag)]
     L.ngrav_gpu_lmac_default_opts.argtypes = [ctypes.POINTER(LmacOpts)]
     L.ngrav_gpu_lmac_set_opts.argtypes = [ctypes.c_void_p, ctypes.POINTER(LmacOpts)]
     L.ngrav_gpu_lmac_default_train_opts.argtypes = [ctypes.POINTER(LmacTrainOpts)]
@@ -302,11 +321,13 @@ class NBodySystem:
     def set_particles(self, x, y, z, vx=None, vy=None, vz=None, m=None):
         arrs = [_c64(a) for a in (x, y, z, vx, vy, vz, m)]
         self.n = len(arrs[0])
+        self.nsys = 1
         self._check(self.L.ngrav_gpu_set_particles(self.h, self.n, *[_p(a, _D) for a in arrs]), self.h)
 
     def set_particles_f32(self, x, y, z, vx, vy, vz, m):
         arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z, vx, vy, vz, m)]
         self.n = len(arrs[0])
+        self.nsys = 1
         self._check(self.L.ngrav_gpu_set_particles_f32(self.h, self.n, *[_p(a, _F) for a in arrs]), self.h)
 
     def set_state(self, x, y, z, vx=None, vy=None, vz=None):
@@ -371,6 +392,49 @@ class NBodySystem:
             _p(t["quad"], _D)), self.h)
         return t
 
+
+    # ---- autotuner ----
+    def autotune(self, reps=2, check_targets=2048, rms_tolerance=1.1, leaf_capacities=None):
+        """Pick leaf capacity, P2P tile and walk stack by timing this state; installs the choice."""
+        o = TuneOpts()
+        self._check(self.L.ngrav_gpu_default_tune_opts(ctypes.byref(o)), None)
+        o.reps, o.check_targets, o.rms_tolerance = reps, check_targets, rms_tolerance
+        if leaf_capacities is not None:
+            for i in range(8):
+                o.leaf_capacities[i] = leaf_capacities[i] if i < len(leaf_capacities) else 0
+        r = TuneReport()
+        self._check(self.L.ngrav_gpu_autotune(self.h, ctypes.byref(o), ctypes.byref(r)), self.h)
+        self.opts.leaf_capacity = r.leaf_capacity
+        tried = [list(r.tried[i]) for i in range(r.ntried)]
+        return dict(leaf_capacity=r.leaf_capacity, p2p_tile=r.p2p_tile, walk_stack=r.walk_stack,
+                    ms_before=r.ms_before, ms_after=r.ms_after, rms_before=r.rms_before, rms_after=r.rms_after,
+                    tried=tried)
+
+    def set_tuning(self, p2p_tile=0, walk_stack=2048):
+        self._check(self.L.ngrav_gpu_set_tuning(self.h, int(p2p_tile), int(walk_stack)), self.h)
+
+    # ---- ensembles ----
+    def set_ensemble(self, offsets):
+        """Treat the particles as independent systems: system s is
+        [offsets[s], offsets[s+1]) of the arrays passed to set_particles."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.nsys = len(off) - 1
+        self._check(self.L.ngrav_gpu_set_ensemble(self.h, self.nsys, off.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int64))), self.h)
+
+    def ensemble_force_error(self, targets_per_system=256, seed=1):
+        k = getattr(self, "nsys", 1)
+        rms, mx = np.zeros(k), np.zeros(k)
+        self._check(self.L.ngrav_gpu_ensemble_force_error(self.h, int(targets_per_system), int(seed), _p(rms, _D),
+                                                          _p(mx, _D)), self.h)
+        return rms, mx
+
+    def ensemble_diagnostics(self, exact_potential=False):
+        k = getattr(self, "nsys", 1)
+        arr = (Diag * k)()
+        self._check(self.L.ngrav_gpu_ensemble_diagnostics(self.h, int(exact_potential), arr), self.h)
+        return [dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
+                     P=list(d.P), potential_exact=bool(d.potential_exact)) for d in arr]
 
     # ---- learned opening test ----
     def lmac_set_opts(self, **kw):

@@ -66,7 +66,7 @@ void free_particles(ngrav_gpu_ctx* ctx) {
 void free_nodes(ngrav_gpu_ctx* ctx) {
     NodeArrays& T = ctx->T;
     dfree(T.start); dfree(T.count); dfree(T.first_child); dfree(T.parent); dfree(T.visit);
-    dfree(T.nchild); dfree(T.level); dfree(T.cx); dfree(T.cy); dfree(T.cz);
+    dfree(T.nchild); dfree(T.level); dfree(T.cx); dfree(T.cy); dfree(T.cz); dfree(T.half); dfree(T.sysroot);
     dfree(T.mass); dfree(T.comx); dfree(T.comy); dfree(T.comz); dfree(T.maxr); dfree(T.quad); dfree(T.amin);
     dfree(T.wA); dfree(T.wB); dfree(T.wC); dfree(T.wD); dfree(T.chi); dfree(T.clo);
     T.cap = 0;
@@ -104,6 +104,7 @@ int alloc_nodes(ngrav_gpu_ctx* ctx, int cap) {
     NG_CUDA(dalloc(T.start, cap)); NG_CUDA(dalloc(T.count, cap)); NG_CUDA(dalloc(T.first_child, cap));
     NG_CUDA(dalloc(T.parent, cap)); NG_CUDA(dalloc(T.visit, cap)); NG_CUDA(dalloc(T.nchild, cap));
     NG_CUDA(dalloc(T.level, cap)); NG_CUDA(dalloc(T.cx, cap)); NG_CUDA(dalloc(T.cy, cap)); NG_CUDA(dalloc(T.cz, cap));
+    NG_CUDA(dalloc(T.half, cap)); NG_CUDA(dalloc(T.sysroot, cap));
     NG_CUDA(dalloc(T.mass, cap)); NG_CUDA(dalloc(T.comx, cap)); NG_CUDA(dalloc(T.comy, cap));
     NG_CUDA(dalloc(T.comz, cap)); NG_CUDA(dalloc(T.maxr, cap)); NG_CUDA(dalloc(T.quad, 5LL * cap));
     NG_CUDA(dalloc(T.amin, cap));
@@ -171,6 +172,8 @@ WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
     wp.stack_cap = ctx->LB.stack_cap;
     wp.node_limit = ctx->T.cap + 32;
     wp.global_stack = ctx->walk_global_stack ? 1 : 0;
+    wp.smem_stack = ctx->walk_stack;
+    wp.p2p_tile = ctx->p2p_tile;
     return wp;
 }
 
@@ -196,7 +199,12 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
         ctx->launches += 2;
     }
     launch_root(ctx->C, n, s);
-    launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->SB.keys, ctx->SB.vals, s);
+    if (ctx->F.nsys > 1) {  // ensemble: every system's own root cube
+        launch_forest_bbox(P.pos, split ? P.plo : nullptr, n, ctx->F, ctx->C, s);
+        launch_forest_root(ctx->F, s);
+        ctx->launches += 2;
+    }
+    launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->F, ctx->SB.keys, ctx->SB.vals, s);
     rec(ctx, 1);
     const int passes = 8;
     radix_sort_pairs(ctx->SB, n, passes, s);
@@ -212,7 +220,7 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     std::swap(P.id, P.id2);
     rec(ctx, 2);
     launch_tree_init(ctx->T, ctx->C, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, s);
-    launch_tree_levels(ctx->T, ctx->C, ctx->SB.keys, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, s);
+    launch_tree_levels(ctx->T, ctx->C, ctx->SB.keys, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, ctx->F, s);
     launch_leaf_list(ctx->T, ctx->C, n, ctx->leaf_at, ctx->flags, ctx->scanbuf, ctx->leaf_list, ctx->SB, s);
     rec(ctx, 3);
     launch_moments(ctx->T, ctx->C, P, ctx->leaf_list, n, (int)std::min<long long>(n, ctx->T.cap), split,
@@ -376,6 +384,7 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
     ctx->have = n > 0;
     ctx->primed = false;
     ctx->acc_valid = false;
+    free_forest(ctx);  // a new particle set is one system until set_ensemble
     return NGRAV_OK;
 }
 
@@ -401,6 +410,9 @@ std::vector<unsigned char> step_key(const ngrav_gpu_ctx* ctx, float hdt, float f
     put(&ctx->opts, sizeof(ctx->opts));
     put(&ctx->walk_global_stack, sizeof(ctx->walk_global_stack));
     put(&ctx->eval_nwarps, sizeof(ctx->eval_nwarps));
+    put(&ctx->F, sizeof(ctx->F));
+    put(&ctx->walk_stack, sizeof(ctx->walk_stack));
+    put(&ctx->p2p_tile, sizeof(ctx->p2p_tile));
     put(&ctx->events, sizeof(ctx->events));
     put(&hdt, sizeof(hdt));
     put(&fdt, sizeof(fdt));
@@ -571,6 +583,7 @@ void ngrav_gpu_destroy(ngrav_gpu_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     drop_graphs(ctx);
     lmac_destroy(ctx);
+    free_forest(ctx);
     free_particles(ctx);
     free_nodes(ctx);
     dfree(ctx->C);
@@ -822,8 +835,9 @@ int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp
     NG_CUDA(cudaStreamSynchronize(ctx->stream));
     NG_CUDA(cudaGetLastError());
     std::vector<float4> acc(nsample);
-    for (int k = 0; k < nsample; ++k)
-        NG_CUDA(cudaMemcpyAsync(&acc[k], ctx->P.acc + slots[k], sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    NG_TRY(ensure_partial(ctx, std::max<long long>(ctx->dpartial_cap, 2LL * nsample)));
+    launch_gather_float4(ctx->P.acc, ctx->dslots, nsample, reinterpret_cast<float4*>(ctx->dpartial), ctx->stream);
+    NG_CUDA(cudaMemcpyAsync(acc.data(), ctx->dpartial, sizeof(float4) * nsample, cudaMemcpyDeviceToHost, ctx->stream));
     NG_CUDA(cudaStreamSynchronize(ctx->stream));
     std::vector<double> rel(nsample);
     double s2 = 0.0, mx = 0.0;
@@ -940,15 +954,14 @@ int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* o
         for (int v = 0; v < nn; ++v)
             if (fc[v] == -1) std::sort(order + st[v], order + st[v] + ct[v]);
     }
-    const double h0 = ctx->hc.root_half;
     std::vector<double> tmp(nn);
     for (int v = 0; v < nn; ++v) {
         if (level) level[v] = lv[v];
         if (prefix) prefix[v] = lv[v] == 0 ? 0ull : (hk[st[v]] >> (3 * (kKeyLevels - lv[v])));
         if (count) count[v] = ct[v];
         if (is_leaf) is_leaf[v] = fc[v] == -1;
-        if (half) half[v] = std::ldexp(h0, -(int)lv[v]);
     }
+    if (half) NG_CUDA(cudaMemcpy(half, ctx->T.half, sizeof(double) * nn, cudaMemcpyDeviceToHost));
     auto get3 = [&](double* dst, const double* a, const double* b, const double* c) -> int {
         if (!dst) return NGRAV_OK;
         const double* src[3] = {a, b, c};

@@ -57,6 +57,14 @@ struct ngrav_gpu_ctx {
     long long cum_evals = 0, cum_pairs = 0, cum_p2c = 0;
     double cum_ms_walk = 0.0, cum_ms_force = 0.0, cum_ms_eval = 0.0, cum_ms_step = 0.0;
     bool acc_valid = false;           // P.acc holds a force evaluation of this particle set
+    int walk_stack = 2048;            // tuned: per-warp shared-memory walk stack entries
+    int p2p_tile = 0;                 // tuned: sources per near batch (0: the kernel's maximum)
+    // ensemble of independent systems (Forest of engine.cuh); nsys = 1: one system
+    Forest F;
+    long long* f_off = nullptr;
+    double* f_root = nullptr;
+    unsigned long long* f_bbox = nullptr;
+    std::vector<long long> h_off;
     // CUDA graphs of one KDK step (kick-drift + force evaluation), keyed by
     // every pointer and parameter the launches bake in; two slots because the
     // particle buffers alternate between steps.
@@ -107,6 +115,9 @@ bool split_of(const ngrav_gpu_ctx* ctx);
 ngrav::WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt);
 // One force evaluation of the current state (retrying on capacity growth).
 int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt);
+int ensure_samp(ngrav_gpu_ctx* ctx, int ns);
+int ensure_partial(ngrav_gpu_ctx* ctx, long long count);
+void free_forest(ngrav_gpu_ctx* ctx);
 
 // Learned opening test hooks (lmac_host.cu).
 void lmac_destroy(ngrav_gpu_ctx* ctx);

@@ -40,4 +40,12 @@ size_t eval_smem_bytes();
 void launch_gather_slots(const int* inv, const int* targets, int nt, int* slots, cudaStream_t s);
 double run_fma_probe(int sm_count, cudaStream_t s);
 
+// ensemble.cu
+void launch_forest_sampler(const Particles& P, bool split, const int* slots, int nslots, const Forest& F,
+                           double eps2, double* out, cudaStream_t s);
+void launch_gather_float4(const float4* a, const int* slots, int ns, float4* out, cudaStream_t s);
+void launch_forest_diag(const Particles& P, bool split, const Forest& F, double* part, cudaStream_t s);
+void launch_forest_potential(const Particles& P, bool split, const Forest& F, double eps2, int chunks, double* part,
+                             cudaStream_t s);
+
 }  // namespace ngrav

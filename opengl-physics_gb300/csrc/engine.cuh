@@ -103,6 +103,8 @@ struct NodeArrays {
     double* cx = nullptr;             // geometric centre (FP64 recurrence of the reference)
     double* cy = nullptr;
     double* cz = nullptr;
+    double* half = nullptr;           // half size (0 on the system-id levels of an ensemble)
+    int* sysroot = nullptr;           // root node of the node's system (0 for a single system)
     // FP64 moments
     double* mass = nullptr;
     double* comx = nullptr;
@@ -169,6 +171,8 @@ struct WalkParams {
     int stack_cap;
     int node_limit;                   // visits per group beyond this mean a corrupt tree
     int global_stack;                 // walk stack in global memory (fallback for deep frontiers)
+    int smem_stack;                   // per-warp shared-memory walk stack: 1024, 2048 or 4096 entries
+    int p2p_tile;                     // sources per near batch of the evaluation (64..256; 0: 256)
     // learned opening test (walk_lmac_kernel)
     int learned;
     float lm_log2b;                   // log2 of the per-target error budget
@@ -179,19 +183,50 @@ struct WalkParams {
     float lm_budget;                  // the budget itself
 };
 
+// A forest of independent systems in one particle set (ensemble).  System s
+// holds slots [off[s], off[s+1]) in every tree order; its id occupies the top
+// sys_levels key digits, the remaining 21 - sys_levels digits are the octant
+// path from its own root cube (the reference's BuildRoot on its particles).
+// The system-id levels are virtual: they always split and carry no geometry.
+// A single system is sys_levels = 0, nsys = 1, off = nullptr.
+struct Forest {
+    int nsys = 1;
+    int sys_levels = 0;
+    const long long* off = nullptr;   // nsys + 1 slot offsets
+    double* root = nullptr;           // per system: centre x, y, z, half (4 doubles)
+    unsigned long long* bbox = nullptr;  // per system: encoded min x, y, z, max x, y, z
+};
+
+// System of a slot (binary search over the offsets).
+__device__ __forceinline__ int forest_system(const Forest& F, long long k) {
+    int lo = 0, hi = F.nsys - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (F.off[mid] <= k)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---- launchers (each enqueues on `s`; no host synchronisation) ----
 void launch_bbox(const float4* pos, const float4* plo, long long n, Counters* C, cudaStream_t s);
 void launch_root(Counters* C, long long n, cudaStream_t s);
+// Ensemble: per-system bounding boxes and root cubes (F.nsys > 1).
+void launch_forest_bbox(const float4* pos, const float4* plo, long long n, const Forest& F, Counters* C,
+                        cudaStream_t s);
+void launch_forest_root(const Forest& F, cudaStream_t s);
 void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s);
-void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, unsigned long long* keys,
-                 unsigned* vals, cudaStream_t s);
+void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F,
+                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
 // Stable LSD radix sort of (keys, vals) over bits [0, 8*passes); result ends
 // in (keys, vals) (the alternates are scratch).
 void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s);
 void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);
 void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s);
 void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
-                        int max_depth, cudaStream_t s);
+                        int max_depth, const Forest& F, cudaStream_t s);
 void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, unsigned* flags, unsigned* scan_out,
                       int* leaf_list, SortBuffers& sb, cudaStream_t s);
 void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,

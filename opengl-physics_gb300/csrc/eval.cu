@@ -272,8 +272,9 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
     // source count fits one staging buffer (so a batch never straddles a
     // 128-entry list chunk).
     const int maxleaf = max(1, C->max_leaf_count);
+    const int tile = wp.p2p_tile > 0 && wp.p2p_tile < kSrcCap ? wp.p2p_tile : kSrcCap;  // tuned batch cap
     int be = 1;
-    while (be < 32 && (be * 2) * maxleaf <= kSrcCap) be *= 2;
+    while (be < 32 && (be * 2) * maxleaf <= tile) be *= 2;
     const bool big_leaves = maxleaf > kSrcCap;
     unsigned long long pairs = 0, p2c = 0;
     bool timeout = false;

@@ -110,6 +110,82 @@ void launch_bbox(const float4* pos, const float4* plo, long long n, Counters* C,
 
 void launch_root(Counters* C, long long n, cudaStream_t s) { root_kernel<<<1, 1, 0, s>>>(C, n); }
 
+// Ensemble: per-system FP64 bounding boxes.  Slots are grouped by system, so a
+// warp whose 32 slots share one system reduces in registers first; mixed warps
+// fall back to per-lane atomics.
+__global__ void __launch_bounds__(kBoxThreads) forest_bbox_kernel(const float4* __restrict__ pos,
+                                                                  const float4* __restrict__ plo, long long n,
+                                                                  Forest F, Counters* C) {
+    const int lane = threadIdx.x & 31;
+    bool bad = false;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const long long i = base + lane;
+        const bool has = i < n;
+        int sys = has ? forest_system(F, i) : -1;
+        double v[3] = {0.0, 0.0, 0.0};
+        if (has) {
+            const float4 p = pos[i];
+            bad |= !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(p.w));
+            for (int a = 0; a < 3; ++a) v[a] = pos_d(p, plo, i, a);
+        }
+        const int s0 = __shfl_sync(0xffffffffu, sys, 0);
+        const bool uniform = __all_sync(0xffffffffu, !has || sys == s0);
+        for (int a = 0; a < 3; ++a) {
+            double l = has ? v[a] : 1.0 / 0.0, h = has ? v[a] : -1.0 / 0.0;
+            if (uniform) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    l = fmin(l, __shfl_xor_sync(0xffffffffu, l, o));
+                    h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+                }
+                if (lane == 0) {
+                    atomicMin(&F.bbox[6 * s0 + a], enc_f64(l));
+                    atomicMax(&F.bbox[6 * s0 + 3 + a], enc_f64(h));
+                }
+            } else if (has) {
+                atomicMin(&F.bbox[6 * sys + a], enc_f64(l));
+                atomicMax(&F.bbox[6 * sys + 3 + a], enc_f64(h));
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&C->status, kStNonFinite);
+}
+
+// BuildRoot (Tree.cpp:54-88) of every system; resets the boxes for the next
+// evaluation.
+__global__ void forest_root_kernel(Forest F) {
+    for (int sys = blockIdx.x * blockDim.x + threadIdx.x; sys < F.nsys; sys += gridDim.x * blockDim.x) {
+        const bool empty = F.off[sys + 1] <= F.off[sys];
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = empty ? 0.0 : dec_f64(F.bbox[6 * sys + a]);
+            hi[a] = empty ? 0.0 : dec_f64(F.bbox[6 * sys + 3 + a]);
+            F.bbox[6 * sys + a] = ~0ull;
+            F.bbox[6 * sys + 3 + a] = 0ull;
+        }
+        double half = __dmul_rn(0.5, __dsub_rn(hi[0], lo[0]));
+        const double hy = __dmul_rn(0.5, __dsub_rn(hi[1], lo[1]));
+        const double hz = __dmul_rn(0.5, __dsub_rn(hi[2], lo[2]));
+        if (half < hy) half = hy;
+        if (half < hz) half = hz;
+        if (!(half > 1e-12)) half = 1.0;
+        for (int a = 0; a < 3; ++a) F.root[4 * sys + a] = __dmul_rn(0.5, __dadd_rn(lo[a], hi[a]));
+        F.root[4 * sys + 3] = __dmul_rn(half, 1.001);
+    }
+}
+
+void launch_forest_bbox(const float4* pos, const float4* plo, long long n, const Forest& F, Counters* C,
+                        cudaStream_t s) {
+    long long blocks = (n + kBoxThreads - 1) / kBoxThreads;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    forest_bbox_kernel<<<(unsigned)blocks, kBoxThreads, 0, s>>>(pos, plo, n, F, C);
+}
+
+void launch_forest_root(const Forest& F, cudaStream_t s) {
+    forest_root_kernel<<<(F.nsys + 127) / 128, 128, 0, s>>>(F);
+}
+
 // SPLIT -> PLAIN: fold the low halves into FP32 positions.
 __global__ void collapse_split_kernel(float4* __restrict__ pos, float4* __restrict__ plo, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -134,11 +210,12 @@ void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s
 // 63-bit keys by the reference's FP64 centre recurrence
 // ---------------------------------------------------------------------------
 
+template <int LEVELS>
 __device__ __forceinline__ unsigned axis_bits(double p, double c, double h) {
-    // Returns 21 octant bits of one axis, level 0 in bit 20.
+    // Returns LEVELS octant bits of one axis, level 0 in the highest bit.
     unsigned bits = 0;
 #pragma unroll
-    for (int l = 0; l < kKeyLevels; ++l) {
+    for (int l = 0; l < LEVELS; ++l) {
         const bool b = p >= c;
         bits = (bits << 1) | (b ? 1u : 0u);
         h = __dmul_rn(0.5, h);
@@ -173,20 +250,57 @@ __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ po
             py += (double)l.y;
             pz += (double)l.z;
         }
-        const unsigned bx = axis_bits(px, cx, h0);
-        const unsigned by = axis_bits(py, cy, h0);
-        const unsigned bz = axis_bits(pz, cz, h0);
+        const unsigned bx = axis_bits<kKeyLevels>(px, cx, h0);
+        const unsigned by = axis_bits<kKeyLevels>(py, cy, h0);
+        const unsigned bz = axis_bits<kKeyLevels>(pz, cz, h0);
         keys[i] = spread3(bx) | (spread3(by) << 1) | (spread3(bz) << 2);
         vals[i] = (unsigned)i;
     }
 }
 
-void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, unsigned long long* keys,
-                 unsigned* vals, cudaStream_t s) {
+// Ensemble keys: the system id in the top SYSL digits, then 21 - SYSL levels
+// of octant path from the system's own root cube.
+template <int SYSL>
+__global__ void __launch_bounds__(256) forest_keys_kernel(const float4* __restrict__ pos,
+                                                          const float4* __restrict__ plo, long long n, Forest F,
+                                                          unsigned long long* __restrict__ keys,
+                                                          unsigned* __restrict__ vals) {
+    constexpr int L = kKeyLevels - SYSL;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int sys = forest_system(F, i);
+        const double cx = F.root[4 * sys], cy = F.root[4 * sys + 1], cz = F.root[4 * sys + 2];
+        const double h0 = F.root[4 * sys + 3];
+        const float4 p = pos[i];
+        double px = p.x, py = p.y, pz = p.z;
+        if (plo) {
+            const float4 l = plo[i];
+            px += (double)l.x;
+            py += (double)l.y;
+            pz += (double)l.z;
+        }
+        const unsigned bx = axis_bits<L>(px, cx, h0);
+        const unsigned by = axis_bits<L>(py, cy, h0);
+        const unsigned bz = axis_bits<L>(pz, cz, h0);
+        keys[i] = ((unsigned long long)sys << (3 * L)) | spread3(bx) | (spread3(by) << 1) | (spread3(bz) << 2);
+        vals[i] = (unsigned)i;
+    }
+}
+
+void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F,
+                 unsigned long long* keys, unsigned* vals, cudaStream_t s) {
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
-    keys_kernel<<<(unsigned)blocks, 256, 0, s>>>(pos, plo, n, C, keys, vals);
+    const unsigned g = (unsigned)blocks;
+    switch (F.sys_levels) {
+        case 0: keys_kernel<<<g, 256, 0, s>>>(pos, plo, n, C, keys, vals); break;
+        case 1: forest_keys_kernel<1><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+        case 2: forest_keys_kernel<2><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+        case 3: forest_keys_kernel<3><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+        case 4: forest_keys_kernel<4><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+        case 5: forest_keys_kernel<5><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+        default: forest_keys_kernel<6><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
+    }
 }
 
 // ---------------------------------------------------------------------------

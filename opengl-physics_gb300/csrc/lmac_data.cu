@@ -49,8 +49,9 @@ __global__ void __launch_bounds__(kRecWarps * 32) lmac_record_kernel(NodeArrays 
         const float4 gD = T.wD[leaf];
         const float gR = T.wC[leaf].x;
         int size = 0;
-        if (leaf != 0) {
-            if (lane == 0) stack[0] = 0;
+        const int root = T.sysroot[leaf];
+        if (leaf != root) {
+            if (lane == 0) stack[0] = root;
             size = 1;
         }
         __syncwarp();

@@ -422,7 +422,7 @@ int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o) {
     o->check_targets = 4096;
     o->revert_rms = 1e-3;
     o->rounds = 3;
-    o->screen = 1.0;
+    o->screen = 10.0;
     return NGRAV_OK;
 }
 

@@ -41,6 +41,8 @@ __global__ void tree_init_kernel(NodeArrays T, Counters* C, long long n, int lea
     T.cx[0] = C->root_center[0];
     T.cy[0] = C->root_center[1];
     T.cz[0] = C->root_center[2];
+    T.half[0] = C->root_half;
+    T.sysroot[0] = 0;
     C->next_free = 1;
     C->level_begin[0] = 0;
     C->level_begin[1] = 1;
@@ -68,16 +70,22 @@ __device__ __forceinline__ int digit_lower_bound(const unsigned long long* __res
 
 constexpr int kLevelThreads = 256;
 
+// One level of the split.  Ensemble (F.sys_levels > 0): levels above
+// sys_levels group systems by id digits, always split and carry no geometry;
+// a child at level sys_levels is a system root and takes that system's cube;
+// below it the reference's recurrence runs from that root.
 __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T, Counters* C,
                                                                    const unsigned long long* __restrict__ keys,
-                                                                   int l, int leaf_cap, int max_depth) {
+                                                                   int l, int leaf_cap, int max_depth, Forest F) {
     const int begin = C->level_begin[l];
     const int end = C->level_begin[l + 1];
     const int shift = 3 * (kKeyLevels - 1 - l);
-    const double child_half = ldexp(C->root_half, -(l + 1));
+    const bool virt = l < F.sys_levels;                 // this level groups systems
+    const bool sys_child = l + 1 == F.sys_levels;      // children are system roots
+    const int depth_cap = max_depth + F.sys_levels;    // max_depth counts from each system root
     for (int node = begin + blockIdx.x * blockDim.x + threadIdx.x; node < end; node += gridDim.x * blockDim.x) {
         const int cnt = T.count[node];
-        if (!(cnt > leaf_cap && l < max_depth)) continue;  // stays a leaf
+        if (!virt && !(cnt > leaf_cap && l < depth_cap)) continue;  // stays a leaf
         const int s = T.start[node];
         const int e = s + cnt;
         int bnd[9];
@@ -98,6 +106,8 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
             continue;
         }
         const double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
+        const double child_half = 0.5 * T.half[node];
+        const int proot = T.sysroot[node];
         int c = base;
 #pragma unroll
         for (int d = 0; d < 8; ++d) {
@@ -110,10 +120,26 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
             T.visit[c] = 0;
             T.nchild[c] = 0;
             T.level[c] = (unsigned char)(l + 1);
-            T.cx[c] = (d & 1) ? __dadd_rn(pcx, child_half) : __dsub_rn(pcx, child_half);
-            T.cy[c] = (d & 2) ? __dadd_rn(pcy, child_half) : __dsub_rn(pcy, child_half);
-            T.cz[c] = (d & 4) ? __dadd_rn(pcz, child_half) : __dsub_rn(pcz, child_half);
-            if (l + 1 >= kKeyLevels && ce - cs > leaf_cap && l + 1 < max_depth) {
+            if (virt) {
+                if (sys_child) {
+                    const int sys = (int)(keys[cs] >> (3 * (kKeyLevels - F.sys_levels)));
+                    T.cx[c] = F.root[4 * sys];
+                    T.cy[c] = F.root[4 * sys + 1];
+                    T.cz[c] = F.root[4 * sys + 2];
+                    T.half[c] = F.root[4 * sys + 3];
+                } else {
+                    T.cx[c] = T.cy[c] = T.cz[c] = 0.0;
+                    T.half[c] = 0.0;
+                }
+                T.sysroot[c] = c;
+            } else {
+                T.cx[c] = (d & 1) ? __dadd_rn(pcx, child_half) : __dsub_rn(pcx, child_half);
+                T.cy[c] = (d & 2) ? __dadd_rn(pcy, child_half) : __dsub_rn(pcy, child_half);
+                T.cz[c] = (d & 4) ? __dadd_rn(pcz, child_half) : __dsub_rn(pcz, child_half);
+                T.half[c] = child_half;
+                T.sysroot[c] = proot;
+            }
+            if (l + 1 >= kKeyLevels && ce - cs > leaf_cap && l + 1 < depth_cap) {
                 atomicOr(&C->status, kStDepthLimit);
                 atomicAdd(&C->depth_limited, 1);
             }
@@ -138,14 +164,14 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
 }
 
 void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
-                        int max_depth, cudaStream_t s) {
+                        int max_depth, const Forest& F, cudaStream_t s) {
     // Enough threads for the widest level (nodes <= cap); levels above it
     // exit after a bounds check.
     long long blocks = ((long long)T.cap / 4 + kLevelThreads - 1) / kLevelThreads;
     if (blocks > 152 * 4) blocks = 152 * 4;
     if (blocks < 1) blocks = 1;
     for (int l = 0; l < kKeyLevels; ++l)
-        tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth);
+        tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth, F);
 }
 
 // ---------------------------------------------------------------------------
@@ -197,11 +223,11 @@ __device__ __forceinline__ float round_up_f(double v) {
 
 __device__ __forceinline__ void write_walk_record(NodeArrays& T, int node, double M, double cx, double cy,
                                                   double cz, const double* Q, double maxr, bool leaf, int link,
-                                                  int cnt_or_nch, int level, double root_half) {
+                                                  int cnt_or_nch, int level) {
     const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
     T.wA[node] = make_float4(hx, hy, hz, (float)M);
     T.wB[node] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
-    const double size = 2.0 * ldexp(root_half, -level);
+    const double size = 2.0 * T.half[node];
     T.wC[node] = make_float4(round_up_f(maxr), (float)size, __int_as_float(link),
                              __int_as_float(meta_pack(leaf, cnt_or_nch, level)));
     T.wD[node] = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy), (float)(cz - (double)hz),
@@ -216,7 +242,6 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
                                                       const float4* __restrict__ acc,
                                                       const int* __restrict__ leaf_list, int split, int quadrupole) {
     const int nleaves = C->nleaves;
-    const double root_half = C->root_half;
     for (int li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
         const int leaf = leaf_list[li];
         const int s = T.start[leaf], cnt = T.count[leaf];
@@ -280,7 +305,7 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         T.amin[leaf] = cnt > 0 ? sqrtf(amin2) : 0.f;
         for (int k = 0; k < 5; ++k) T.quad[5 * leaf + k] = Q[k];
         const int level = T.level[leaf];
-        write_walk_record(T, leaf, M, cx, cy, cz, Q, maxr, true, s, cnt, level, root_half);
+        write_walk_record(T, leaf, M, cx, cy, cz, Q, maxr, true, s, cnt, level);
         const float hx = (float)ccx, hy = (float)ccy, hz = (float)ccz;
         T.chi[leaf] = make_float4(hx, hy, hz, 0.f);
         T.clo[leaf] = make_float4((float)(ccx - (double)hx), (float)(ccy - (double)hy), (float)(ccz - (double)hz), 0.f);
@@ -297,7 +322,6 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
                                                               int quadrupole) {
     const int begin = C->level_begin[l];
     const int end = C->level_begin[l + 1];
-    const double root_half = C->root_half;
     for (int node = begin + blockIdx.x * blockDim.x + threadIdx.x; node < end; node += gridDim.x * blockDim.x) {
         const int fc = T.first_child[node];
         if (fc < 0) continue;
@@ -344,7 +368,7 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
         T.comz[node] = pcz;
         T.maxr[node] = mr;
         for (int k = 0; k < 5; ++k) T.quad[5 * node + k] = PQ[k];
-        write_walk_record(T, node, PM, pcx, pcy, pcz, PQ, mr, false, fc, nch, l, root_half);
+        write_walk_record(T, node, PM, pcx, pcy, pcz, PQ, mr, false, fc, nch, l);
     }
 }
 

@@ -40,23 +40,21 @@ constexpr int kWalkWarps = 4;
 constexpr int kWalkThreads = kWalkWarps * 32;
 constexpr int kNPL = 2;  // nodes tested per lane per iteration (memory-level parallelism)
 
-constexpr int kSmemStack = 2048;  // per-warp traversal stack in shared memory (8 KiB)
-
-// SMEM_STACK: the traversal stack lives in shared memory (push -> pop never
-// leaves the SM); the global-memory variant is the fallback for trees whose
-// frontier outgrows it.
-template <bool SMEM_STACK>
+// STACK > 0: a per-warp traversal stack of STACK entries in shared memory
+// (push -> pop never leaves the SM; the size trades occupancy against the
+// frontier it holds, a tuned choice); STACK = 0: the global-memory stack, the
+// fallback for trees whose frontier outgrows shared memory.
+template <int STACK>
 __global__ void __launch_bounds__(kWalkThreads) walk_kernel(NodeArrays T, Counters* C,
                                                             const int* __restrict__ leaf_list, WalkParams wp,
                                                             ListBuffers LB) {
-    __shared__ int s_stack[SMEM_STACK ? kWalkWarps * kSmemStack : 1];
+    __shared__ int s_stack[STACK > 0 ? kWalkWarps * STACK : 1];
     const int lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * kWalkWarps + (threadIdx.x >> 5);
     if (C->status & kStFatal) return;
-    int* stack = SMEM_STACK ? s_stack + (threadIdx.x >> 5) * kSmemStack : LB.stack + (long long)gwarp * LB.stack_cap;
-    const int stack_cap = SMEM_STACK ? kSmemStack : LB.stack_cap;
+    int* stack = STACK > 0 ? s_stack + (threadIdx.x >> 5) * STACK : LB.stack + (long long)gwarp * LB.stack_cap;
+    const int stack_cap = STACK > 0 ? STACK : LB.stack_cap;
     const int nleaves = C->nleaves;
-    const double root_half = C->root_half;
     const unsigned lt_mask = (1u << lane) - 1u;
     unsigned long long tests = 0, retests = 0, groups = 0;
     int stack_max = 0, list_max = 0;
@@ -86,8 +84,9 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(NodeArrays T, Counte
         list_append(near, lane == 0, leaf, LB.near, LB.near_next, &C->near_chunks, LB.near_chunk_cap, lane,
                     lt_mask, bad);
         int size = 0;
-        if (leaf != 0) {
-            if (lane == 0) stack[0] = 0;
+        const int root = T.sysroot[leaf];
+        if (leaf != root) {
+            if (lane == 0) stack[0] = root;
             size = 1;
         }
         int visits = 0;
@@ -149,7 +148,7 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(NodeArrays T, Counte
                                 const double ex = T.comx[nd] - gcx_d, ey = T.comy[nd] - gcy_d,
                                              ez = T.comz[nd] - gcz_d;
                                 const double d2 = ex * ex + ey * ey + ez * ez;
-                                const double sz = 2.0 * ldexp(root_half, -((meta >> 24) & 31));
+                                const double sz = 2.0 * T.half[nd];
                                 const double w = sqrt(d2) - gr_d;
                                 accept = w > 0.0 && sz * sz < wp.theta2_d * w * w;
                             }
@@ -218,9 +217,9 @@ int walk_warps_per_block() { return kWalkWarps; }
 
 int walk_blocks_per_sm() {
     int nb = 0, ng = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, walk_kernel<true>, kWalkThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ng, walk_kernel<false>, kWalkThreads, 0);
-    nb = nb < ng ? nb : ng;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, walk_kernel<1024>, kWalkThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ng, walk_kernel<0>, kWalkThreads, 0);
+    nb = nb > ng ? nb : ng;
     return nb > 0 ? nb : 1;
 }
 
@@ -228,9 +227,13 @@ void launch_walk(const NodeArrays& T, Counters* C, const int* leaf_list, const W
                  const ListBuffers& LB, cudaStream_t s) {
     const int blocks = (LB.nwarps + kWalkWarps - 1) / kWalkWarps;
     if (wp.global_stack)
-        walk_kernel<false><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
+        walk_kernel<0><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
+    else if (wp.smem_stack == 1024)
+        walk_kernel<1024><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
+    else if (wp.smem_stack == 4096)
+        walk_kernel<4096><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
     else
-        walk_kernel<true><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
+        walk_kernel<2048><<<blocks, kWalkThreads, 0, s>>>(T, C, leaf_list, wp, LB);
 }
 
 }  // namespace ngrav

@@ -144,8 +144,9 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
             near = {-1, -1, 0, 0, nres_next, nres_end};
             list_append(near, lane == 0, leaf, LB.near, LB.near_next, &C->near_chunks, LB.near_chunk_cap, lane,
                         lt_mask, bad);
-            if (leaf != 0) {
-                if (lane == 0) stack[0] = 0;
+            const int root = T.sysroot[leaf];
+            if (leaf != root) {
+                if (lane == 0) stack[0] = root;
                 size = 1;
             }
         } else {

@@ -49,14 +49,16 @@ def test_struct_layouts_match_header(pkg, tmp_path):
         " sizeof(ngrav_gpu_diag), sizeof(ngrav_gpu_ferr), sizeof(ngrav_gpu_stats), offsetof(ngrav_gpu_opts, G),"
         " offsetof(ngrav_gpu_stats, p2p_pairs), offsetof(ngrav_gpu_stats, lmac_last_check_rms),"
         " sizeof(ngrav_gpu_lmac_opts), sizeof(ngrav_gpu_lmac_train_opts), offsetof(ngrav_gpu_lmac_train_opts, seed),"
-        " sizeof(ngrav_gpu_lmac_report));return 0;}\n")
+        " sizeof(ngrav_gpu_lmac_report)); printf(\"%zu %zu %zu\\n\", sizeof(ngrav_gpu_tune_opts),"
+        " sizeof(ngrav_gpu_tune_report), offsetof(ngrav_gpu_tune_report, tried));return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(pkg.Opts), ctypes.sizeof(pkg.Diag), ctypes.sizeof(pkg.Ferr), ctypes.sizeof(pkg.Stats),
             pkg.Opts.G.offset, pkg.Stats.p2p_pairs.offset, pkg.Stats.lmac_last_check_rms.offset,
             ctypes.sizeof(pkg.LmacOpts), ctypes.sizeof(pkg.LmacTrainOpts), pkg.LmacTrainOpts.seed.offset,
-            ctypes.sizeof(pkg.LmacReport)]
+            ctypes.sizeof(pkg.LmacReport), ctypes.sizeof(pkg.TuneOpts), ctypes.sizeof(pkg.TuneReport),
+            pkg.TuneReport.tried.offset]
     assert got == want
 
 
