@@ -55,6 +55,8 @@ WORKLOADS = {
     "galaxy1m": ("galaxy", {"n_halo": 943718, "n_disk": 104858}, 0.002, 2e-4, 0.6, 16),
     "plummer1m": ("plummer", {"n": 1048576, "seed": 1}, 0.005, 5e-4, 0.5, 16),
     "plummer16k": ("plummer", {"n": 16384, "seed": 0}, 0.01, 1e-3, 0.5, 16),
+    # 512 Plummer spheres, N_i log-uniform in [1024, 65536] (~7.9M), one launch per phase
+    "ensemble512": ("ensemble", {"nsys": 512}, 0.01, 1e-3, 0.6, 16),
 }
 # DRAM bytes (read + write) per interaction-list entry of one eval_kernel launch,
 # from dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture at
@@ -120,7 +122,54 @@ class ClockSampler:
 def make_inputs(pkg_ic, workload):
     gen, kw, eps, dt, theta, ncrit = WORKLOADS[workload]
     arrs = getattr(pkg_ic, gen)(**kw)
+    if gen == "ensemble":
+        arrs = arrs[0]  # offsets: see run_ensemble
     return arrs, eps, dt, theta, ncrit
+
+
+def run_ensemble(args, pkg, ic, rank, world, dev):
+    """Ensemble of independent systems: autotuned leaf capacity, one launch per
+    phase for all systems, CUDA-graph steps; per-system error on 256 targets."""
+    gen, kw, eps, dt, theta, ncrit = WORKLOADS[args.workload]
+    arrs, off = ic.ensemble(**kw)
+    n, nsys = len(arrs[0]), len(off) - 1
+    sim = pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=ncrit, device=dev,
+                          timing=True)
+    sim.set_particles_f32(*arrs)
+    sim.set_ensemble(off)
+    sim.prime()
+    tune = sim.autotune(reps=2, check_targets=4096)
+    sim.prime()
+    clocks = ClockSampler(dev)
+    st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks)
+    rms, mx = sim.ensemble_force_error(256, seed=1)
+    value = world * n / (ms_step * 1e-3)
+    flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
+    achieved = flops / (st["cum_ms_force"] * 1e-3) / 1e12 if st["cum_ms_force"] > 0 else None
+    peak = pkg.probe_fp32_peak(dev)
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s, ensemble of 512 Plummer spheres (log-uniform N in [1024, 65536])",
+            "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Plummer generator, system i seed i)",
+            "config": {"workload": args.workload, "n": n, "systems": nsys, "n_min": int(np.diff(off).min()),
+                       "n_max": int(np.diff(off).max()), "eps": eps, "theta": theta, "dt": dt,
+                       "leaf_capacity": tune["leaf_capacity"], "autotune": tune, "graph_replays": st["graph_replays"],
+                       "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
+                       "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
+                       "ms_phases_last_eval": phases(st),
+                       "per_system_force_err_rms": {"median": float(np.median(rms)), "max": float(rms.max()),
+                                                    "targets_per_system": 256},
+                       "per_system_force_err_max": float(mx.max())},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                         "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)"},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": st["cum_launches"], "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    return 0
 
 
 def cpu_baseline(orc, arrs, eps, theta, ncrit, target_s=15.0):
@@ -235,6 +284,8 @@ def main():
     pkg = ge.load_package()
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"])
     dev = local
+    if WORKLOADS[args.workload][0] == "ensemble":
+        return run_ensemble(args, pkg, ic, rank, world, dev)
     arrs, eps, dt, theta0, ncrit = make_inputs(ic, args.workload)
     n = len(arrs[0])
     prec = pkg.PRECISION_SPLIT if args.precision == "split" else pkg.PRECISION_PLAIN

@@ -50,6 +50,11 @@ enum {
     NGRAV_ERR_DEPTH = 8          /* strict_depth set and a leaf needs more than 21 levels */
 };
 
+/* Softening kernel (include/ngrav/Softening.hpp:30-33): Plummer with length
+ * eps, or the Hernquist & Katz cubic spline with smoothing length h = eps
+ * (exactly Newtonian beyond 2 eps). */
+enum { NGRAV_SOFTENING_PLUMMER = 0, NGRAV_SOFTENING_SPLINE = 1 };
+
 /* Multipole acceptance criterion (include/ngrav/Mac.hpp:8-11). */
 enum { NGRAV_MAC_GEOMETRIC = 0, NGRAV_MAC_LEARNED = 1 };
 
@@ -156,6 +161,11 @@ int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, cons
 /* FP32 variant: no conversion, for large N. */
 int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
                                 const float* vx, const float* vy, const float* vz, const float* m);
+
+/* Softening of every pair force, far-field monopole and potential
+ * (Softening::Plummer / Softening::Spline, include/ngrav/Softening.hpp:120-140);
+ * the quadrupole term stays unsoftened, as in AddQuadrupole. */
+int ngrav_gpu_set_softening(ngrav_gpu_ctx* ctx, int kind);
 
 /* New positions (and velocities, unless NULL) for the particles already set,
  * in the caller's order; masses stay, and so do the accelerations of the last

@@ -15,6 +15,7 @@
 #include "ctx_internal.cuh"
 #include "ctx_kernels.cuh"
 #include "engine.cuh"
+#include "softening.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -173,6 +174,8 @@ WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt) {
     wp.node_limit = ctx->T.cap + 32;
     wp.global_stack = ctx->walk_global_stack ? 1 : 0;
     wp.smem_stack = ctx->walk_stack;
+    wp.soft = ctx->soft;
+    wp.ih = ctx->opts.eps > 0.0 ? (float)(1.0 / ctx->opts.eps) : 0.f;
     wp.p2p_tile = ctx->p2p_tile;
     return wp;
 }
@@ -412,6 +415,7 @@ std::vector<unsigned char> step_key(const ngrav_gpu_ctx* ctx, float hdt, float f
     put(&ctx->eval_nwarps, sizeof(ctx->eval_nwarps));
     put(&ctx->F, sizeof(ctx->F));
     put(&ctx->walk_stack, sizeof(ctx->walk_stack));
+    put(&ctx->soft, sizeof(ctx->soft));
     put(&ctx->p2p_tile, sizeof(ctx->p2p_tile));
     put(&ctx->events, sizeof(ctx->events));
     put(&hdt, sizeof(hdt));
@@ -643,6 +647,17 @@ int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, c
 }
 
 
+int ngrav_gpu_set_softening(ngrav_gpu_ctx* ctx, int kind) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (kind != NGRAV_SOFTENING_PLUMMER && kind != NGRAV_SOFTENING_SPLINE)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "unknown softening kind");
+    if (kind == NGRAV_SOFTENING_SPLINE && !(ctx->opts.eps > 0.0))
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "spline softening needs eps > 0");
+    ctx->soft = kind == NGRAV_SOFTENING_SPLINE ? kSoftSpline : kSoftPlummer;
+    ctx->primed = false;
+    return NGRAV_OK;
+}
+
 int ngrav_gpu_set_state(ngrav_gpu_ctx* ctx, const double* x, const double* y, const double* z, const double* vx,
                         const double* vy, const double* vz) {
     if (!ctx) return NGRAV_ERR_INVALID_ARG;
@@ -780,7 +795,7 @@ int ngrav_gpu_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_dia
     const bool exact = exact_potential || n <= 262144;
     out->potential_exact = exact ? 1 : 0;
     if (exact) {
-        launch_potential(n, ctx->P, split, ctx->opts.eps * ctx->opts.eps, ctx->dpartial, ctx->stream);
+        launch_potential(n, ctx->P, split, ctx->opts.eps * ctx->opts.eps, spline_h(ctx), ctx->dpartial, ctx->stream);
         NG_CUDA(cudaMemcpyAsync(h.data(), ctx->dpartial, sizeof(double) * npb, cudaMemcpyDeviceToHost,
                                 ctx->stream));
         NG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -823,10 +838,15 @@ int ngrav_gpu_force_error(ngrav_gpu_ctx* ctx, int nsample, uint64_t seed, int fp
                             ctx->stream));
     launch_inverse_id(n, ctx->P.id, ctx->inv, ctx->stream);
     launch_gather_slots(ctx->inv, ctx->dtargets, nsample, ctx->dslots, ctx->stream);
-    const int shares = sampler_shares(n, nsample, ctx->sm_count);
-    NG_TRY(ensure_partial(ctx, 3LL * shares * nsample));
-    launch_sampler(n, ctx->P, split_of(ctx), ctx->dslots, nsample, ctx->opts.eps * ctx->opts.eps, fp64_pairs != 0,
-                   ctx->dsamp, ctx->dpartial, shares, ctx->stream);
+    if (ctx->F.nsys > 1) {  // ensemble: each target against its own system only
+        launch_forest_sampler(ctx->P, split_of(ctx), ctx->dslots, nsample, ctx->F, ctx->opts.eps * ctx->opts.eps,
+                              spline_h(ctx), ctx->dsamp, ctx->stream);
+    } else {
+        const int shares = sampler_shares(n, nsample, ctx->sm_count);
+        NG_TRY(ensure_partial(ctx, 3LL * shares * nsample));
+        launch_sampler(n, ctx->P, split_of(ctx), ctx->dslots, nsample, ctx->opts.eps * ctx->opts.eps, spline_h(ctx),
+                       fp64_pairs != 0, ctx->dsamp, ctx->dpartial, shares, ctx->stream);
+    }
     std::vector<double> ref(3 * (size_t)nsample);
     std::vector<int> slots(nsample);
     NG_CUDA(cudaMemcpyAsync(ref.data(), ctx->dsamp, sizeof(double) * 3 * nsample, cudaMemcpyDeviceToHost,

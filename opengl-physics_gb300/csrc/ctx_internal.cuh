@@ -59,6 +59,7 @@ struct ngrav_gpu_ctx {
     bool acc_valid = false;           // P.acc holds a force evaluation of this particle set
     int walk_stack = 2048;            // tuned: per-warp shared-memory walk stack entries
     int p2p_tile = 0;                 // tuned: sources per near batch (0: the kernel's maximum)
+    int soft = 0;                     // kSoftPlummer / kSoftSpline (softening.cuh)
     // ensemble of independent systems (Forest of engine.cuh); nsys = 1: one system
     Forest F;
     long long* f_off = nullptr;
@@ -112,6 +113,8 @@ cudaError_t dalloc(T*& p, long long count) {
 
 int fail(ngrav_gpu_ctx* ctx, int code, const std::string& msg);
 bool split_of(const ngrav_gpu_ctx* ctx);
+// Smoothing length of the spline softening, 0 with Plummer softening.
+inline double spline_h(const ngrav_gpu_ctx* ctx) { return ctx->soft == 1 ? ctx->opts.eps : 0.0; }
 ngrav::WalkParams walk_params(const ngrav_gpu_ctx* ctx, bool kick, float hdt);
 // One force evaluation of the current state (retrying on capacity growth).
 int evaluate(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt);

@@ -23,12 +23,13 @@ void launch_diag_pass1(long long n, const Particles& P, bool split, double* part
 void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, double cy, double cz, double* partial,
                        cudaStream_t s);
 int potential_blocks(long long n);
-void launch_potential(long long n, const Particles& P, bool split, double eps2, double* partial, cudaStream_t s);
+void launch_potential(long long n, const Particles& P, bool split, double eps2, double spline_h, double* partial,
+                      cudaStream_t s);
 int sampler_shares(long long n, int nslots, int sm_count);
 // FP64 pairs (one block per target), or FP32 pairs tiled over `shares`
 // source shares with FP64 totals (partial: shares * 3 * nslots doubles).
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
-                    bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s);
+                    double spline_h, bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s);
 void launch_reset_counters(Counters* C, cudaStream_t s);
 void eval_set_attributes();
 void lmac_set_attributes();
@@ -42,7 +43,7 @@ double run_fma_probe(int sm_count, cudaStream_t s);
 
 // ensemble.cu
 void launch_forest_sampler(const Particles& P, bool split, const int* slots, int nslots, const Forest& F,
-                           double eps2, double* out, cudaStream_t s);
+                           double eps2, double spline_h, double* out, cudaStream_t s);
 void launch_gather_float4(const float4* a, const int* slots, int ns, float4* out, cudaStream_t s);
 void launch_forest_diag(const Particles& P, bool split, const Forest& F, double* part, cudaStream_t s);
 void launch_forest_potential(const Particles& P, bool split, const Forest& F, double eps2, int chunks, double* part,

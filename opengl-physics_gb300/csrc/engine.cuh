@@ -172,6 +172,8 @@ struct WalkParams {
     int node_limit;                   // visits per group beyond this mean a corrupt tree
     int global_stack;                 // walk stack in global memory (fallback for deep frontiers)
     int smem_stack;                   // per-warp shared-memory walk stack: 1024, 2048 or 4096 entries
+    int soft;                         // kSoftPlummer or kSoftSpline (softening.cuh)
+    float ih;                         // spline: 1 / h (h = eps)
     int p2p_tile;                     // sources per near batch of the evaluation (64..256; 0: 256)
     // learned opening test (walk_lmac_kernel)
     int learned;

@@ -10,6 +10,7 @@
 // the learned opening test need nothing else.
 #include "ctx_internal.cuh"
 #include "ctx_kernels.cuh"
+#include "softening.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -21,10 +22,11 @@ namespace ngrav {
 
 // Direct sum of each target's own system, FP32 pairs, FP64 totals; one block
 // per target.
+template <int SOFT>
 __global__ void __launch_bounds__(256) forest_sampler_kernel(const float4* __restrict__ pos,
                                                              const float4* __restrict__ plo,
                                                              const int* __restrict__ slots, Forest F, float eps2,
-                                                             double* __restrict__ out) {
+                                                             float ih, double* __restrict__ out) {
     __shared__ double red[3][8];
     const int ti = slots[blockIdx.x];
     const int sys = forest_system(F, ti);
@@ -43,9 +45,7 @@ __global__ void __launch_bounds__(256) forest_sampler_kernel(const float4* __res
             const float dx = (p.x - tp.x) + (l.x - tl.x);
             const float dy = (p.y - tp.y) + (l.y - tl.y);
             const float dz = (p.z - tp.z) + (l.z - tl.z);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            const float inv = rsqrtf(r2);
-            const float f = p.w * inv * inv * inv;
+            const float f = pair_factor<SOFT>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), p.w, eps2, ih);
             px = fmaf(f, dx, px);
             py = fmaf(f, dy, py);
             pz = fmaf(f, dz, pz);
@@ -172,9 +172,14 @@ __global__ void __launch_bounds__(256) forest_potential_kernel(const float4* __r
 }
 
 void launch_forest_sampler(const Particles& P, bool split, const int* slots, int nslots, const Forest& F,
-                           double eps2, double* out, cudaStream_t s) {
+                           double eps2, double spline_h, double* out, cudaStream_t s) {
     if (nslots <= 0) return;
-    forest_sampler_kernel<<<nslots, 256, 0, s>>>(P.pos, split ? P.plo : nullptr, slots, F, (float)eps2, out);
+    if (spline_h > 0.0)
+        forest_sampler_kernel<kSoftSpline><<<nslots, 256, 0, s>>>(P.pos, split ? P.plo : nullptr, slots, F, 0.f,
+                                                                 (float)(1.0 / spline_h), out);
+    else
+        forest_sampler_kernel<kSoftPlummer><<<nslots, 256, 0, s>>>(P.pos, split ? P.plo : nullptr, slots, F,
+                                                                  (float)eps2, 0.f, out);
 }
 
 void launch_forest_diag(const Particles& P, bool split, const Forest& F, double* part, cudaStream_t s) {
@@ -286,8 +291,8 @@ int ngrav_gpu_ensemble_force_error(ngrav_gpu_ctx* ctx, int targets_per_system, u
         NG_CUDA(cudaMemcpy(d_one, one_off, sizeof(one_off), cudaMemcpyHostToDevice));
         F.off = d_one;
     }
-    launch_forest_sampler(ctx->P, split_of(ctx), ctx->dslots, nt, F, ctx->opts.eps * ctx->opts.eps, ctx->dsamp,
-                          ctx->stream);
+    launch_forest_sampler(ctx->P, split_of(ctx), ctx->dslots, nt, F, ctx->opts.eps * ctx->opts.eps, spline_h(ctx),
+                          ctx->dsamp, ctx->stream);
     launch_gather_float4(ctx->P.acc, ctx->dslots, nt, reinterpret_cast<float4*>(ctx->dpartial), ctx->stream);
     std::vector<double> ref(3 * (size_t)nt);
     std::vector<float4> acc(nt);

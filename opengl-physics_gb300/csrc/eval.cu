@@ -21,6 +21,7 @@
 // resident warps; measured slower.)  In SPLIT precision each lane's partial
 // sums are Kahan compensated once per staged chunk.
 #include "engine.cuh"
+#include "softening.cuh"
 
 namespace ngrav {
 
@@ -125,8 +126,9 @@ __device__ __forceinline__ void accumulate(Lane& g, float px, float py, float pz
     }
 }
 
-template <bool SPLIT, bool ZEROSOFT>
-__device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_src, int ns, float eps2) {
+// SOFT: 0 Plummer, 1 Plummer with eps = 0 (the self pair gives 0), 2 spline.
+template <bool SPLIT, int SOFT>
+__device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_src, int ns, float eps2, float ih) {
     if (!g.active) return;
     float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
     const float tx = g.tx, ty = g.ty, tz = g.tz;
@@ -137,13 +139,20 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_
         const float4 b = s_src[j + S];
         const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
         const float bx_ = b.x - tx, by_ = b.y - ty, bz_ = b.z - tz;
-        const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
-        const float rb = fmaf(bx_, bx_, fmaf(by_, by_, fmaf(bz_, bz_, eps2)));
-        const float ia = rsqrtf(ra), ib = rsqrtf(rb);
-        float fa = a.w * (ia * ia * ia), fb = b.w * (ib * ib * ib);
-        if (ZEROSOFT) {
-            fa = ra > 0.f ? fa : 0.f;
-            fb = rb > 0.f ? fb : 0.f;
+        float fa, fb;
+        if (SOFT == 2) {
+            fa = pair_factor<kSoftSpline>(fmaf(ax_, ax_, fmaf(ay_, ay_, az_ * az_)), a.w, 0.f, ih);
+            fb = pair_factor<kSoftSpline>(fmaf(bx_, bx_, fmaf(by_, by_, bz_ * bz_)), b.w, 0.f, ih);
+        } else {
+            const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
+            const float rb = fmaf(bx_, bx_, fmaf(by_, by_, fmaf(bz_, bz_, eps2)));
+            const float ia = rsqrtf(ra), ib = rsqrtf(rb);
+            fa = a.w * (ia * ia * ia);
+            fb = b.w * (ib * ib * ib);
+            if (SOFT == 1) {
+                fa = ra > 0.f ? fa : 0.f;
+                fb = rb > 0.f ? fb : 0.f;
+            }
         }
         px = fmaf(fa, ax_, px);
         py = fmaf(fa, ay_, py);
@@ -155,10 +164,15 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_
     if (j < ns) {
         const float4 a = s_src[j];
         const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
-        const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
-        const float ia = rsqrtf(ra);
-        float fa = a.w * (ia * ia * ia);
-        if (ZEROSOFT) fa = ra > 0.f ? fa : 0.f;
+        float fa;
+        if (SOFT == 2) {
+            fa = pair_factor<kSoftSpline>(fmaf(ax_, ax_, fmaf(ay_, ay_, az_ * az_)), a.w, 0.f, ih);
+        } else {
+            const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
+            const float ia = rsqrtf(ra);
+            fa = a.w * (ia * ia * ia);
+            if (SOFT == 1) fa = ra > 0.f ? fa : 0.f;
+        }
         px = fmaf(fa, ax_, px);
         py = fmaf(fa, ay_, py);
         pz = fmaf(fa, az_, pz);
@@ -166,9 +180,9 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_
     accumulate<SPLIT>(g, px + qx, py + qy, pz + qz);
 }
 
-template <bool SPLIT, bool QUAD>
+template <bool SPLIT, bool QUAD, int SOFT>
 __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA, const float4* __restrict__ fB,
-                                          const float* __restrict__ fQ, int nf, float eps2) {
+                                          const float* __restrict__ fQ, int nf, float eps2, float ih) {
     if (!g.active) return;
     float px = 0.f, py = 0.f, pz = 0.f;
     const float tx = g.tx, ty = g.ty, tz = g.tz;
@@ -176,8 +190,7 @@ __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA
         const float4 A = fA[f];
         const float dx = A.x - tx, dy = A.y - ty, dz = A.z - tz;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float rs = rsqrtf(r2 + eps2);
-        const float fm = A.w * (rs * rs * rs);
+        const float fm = pair_factor<SOFT == 2 ? kSoftSpline : kSoftPlummer>(r2, A.w, eps2, ih);
         px = fmaf(fm, dx, px);
         py = fmaf(fm, dy, py);
         pz = fmaf(fm, dz, pz);
@@ -251,7 +264,7 @@ __device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& 
     return tot;
 }
 
-template <bool SPLIT, bool QUAD, bool ZEROSOFT>
+template <bool SPLIT, bool QUAD, int SOFT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
                                                             float4* __restrict__ acc, float4* __restrict__ vel,
@@ -342,7 +355,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                             if (QUAD) B = T.wB[node];
                         }
                     }
-                    p2c_chunk<SPLIT, QUAD>(g, sm.farA, sm.farB, sm.farQ, min(32, nfar - b), wp.eps2);
+                    p2c_chunk<SPLIT, QUAD, SOFT>(g, sm.farA, sm.farB, sm.farQ, min(32, nfar - b), wp.eps2, wp.ih);
                     __syncwarp();
                 }
             }
@@ -391,7 +404,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                             }
                         }
                         __syncwarp();
-                        p2p_chunk<SPLIT, ZEROSOFT>(g, sm.src[bcur], ns_cur, wp.eps2);
+                        p2p_chunk<SPLIT, SOFT>(g, sm.src[bcur], ns_cur, wp.eps2, wp.ih);
                         __syncwarp();
                     }
                     total += ns_cur;
@@ -438,7 +451,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                             sm.src[0][j] = v;
                         }
                         __syncwarp();
-                        p2p_chunk<SPLIT, ZEROSOFT>(g, sm.src[0], ns, wp.eps2);
+                        p2p_chunk<SPLIT, SOFT>(g, sm.src[0], ns, wp.eps2, wp.ih);
                     }
                     __syncwarp();
                     total += cn;
@@ -490,9 +503,10 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
 size_t eval_smem_bytes() { return sizeof(EvalSmem) * kEvalWarps; }
 int eval_warps_per_block() { return kEvalWarps; }
 
-#define NGRAV_EVAL_INSTANCES(X) \
-    X(true, true, true) X(true, true, false) X(true, false, true) X(true, false, false) \
-    X(false, true, true) X(false, true, false) X(false, false, true) X(false, false, false)
+#define NGRAV_EVAL_INSTANCES(X)                                                       \
+    X(true, true, 0) X(true, true, 1) X(true, true, 2) X(true, false, 0) X(true, false, 1) \
+    X(true, false, 2) X(false, true, 0) X(false, true, 1) X(false, true, 2) X(false, false, 0) \
+    X(false, false, 1) X(false, false, 2)
 
 void eval_set_attributes() {
     const int bytes = (int)eval_smem_bytes();
@@ -504,7 +518,7 @@ void eval_set_attributes() {
 
 int eval_blocks_per_sm() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_kernel<true, true, false>, kEvalThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, eval_kernel<true, true, 0>, kEvalThreads,
                                                   eval_smem_bytes());
     return nb > 0 ? nb : 1;
 }
@@ -512,10 +526,10 @@ int eval_blocks_per_sm() {
 void launch_eval(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, const WalkParams& wp,
                  const ListBuffers& LB, int nwarps, cudaStream_t s) {
     const int blocks = (nwarps + kEvalWarps - 1) / kEvalWarps;
-    const bool zs = !(wp.eps2 > 0.f);
+    const int soft = wp.soft == kSoftSpline ? 2 : (!(wp.eps2 > 0.f) ? 1 : 0);
     const size_t smem = eval_smem_bytes();
 #define NGRAV_LAUNCH(SP, Q, Z)                                                                             \
-    if (wp.split == (SP) && (wp.quadrupole != 0) == (Q) && zs == (Z))                                     \
+    if (wp.split == (SP) && (wp.quadrupole != 0) == (Q) && soft == (Z))                                   \
         eval_kernel<SP, Q, Z><<<blocks, kEvalThreads, smem, s>>>(T, C, P.src, P.acc, P.vel, leaf_list, wp, LB);
     NGRAV_EVAL_INSTANCES(NGRAV_LAUNCH)
 #undef NGRAV_LAUNCH

@@ -14,6 +14,7 @@
 // fixed order (deterministic); the potential is the exact FP64 pair sum
 // sum_{i<j} -G m_i m_j / sqrt(r^2 + eps^2).
 #include "engine.cuh"
+#include "softening.cuh"
 #include "ctx_kernels.cuh"
 
 namespace ngrav {
@@ -324,9 +325,11 @@ void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, d
 // Exact pair potential: thread i sums j > i over shared-memory tiles, in FP64.
 constexpr int kPotThreads = 256;
 
+// spline_h > 0: the spline pair potential of smoothing length spline_h
+// (softening.cuh); else Plummer with eps2.
 __global__ void __launch_bounds__(kPotThreads) potential_kernel(long long n, const float4* __restrict__ pos,
                                                                 const float4* __restrict__ plo, double eps2,
-                                                                double* __restrict__ partial) {
+                                                                double spline_h, double* __restrict__ partial) {
     __shared__ double sx[kPotThreads], sy[kPotThreads], sz[kPotThreads], sm[kPotThreads];
     __shared__ double red[32];
     const long long i = blockIdx.x * (long long)kPotThreads + threadIdx.x;
@@ -369,8 +372,13 @@ __global__ void __launch_bounds__(kPotThreads) potential_kernel(long long n, con
             for (int k = 0; k < kmax; ++k) {
                 if (t + k <= i) continue;
                 const double dx = sx[k] - xi, dy = sy[k] - yi, dz = sz[k] - zi;
-                const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-                local -= sm[k] * rsqrt(r2);
+                if (spline_h > 0.0) {
+                    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                    local += sm[k] * spline_phi_d(r / spline_h) / spline_h;
+                } else {
+                    const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                    local -= sm[k] * rsqrt(r2);
+                }
             }
         }
     }
@@ -381,8 +389,10 @@ __global__ void __launch_bounds__(kPotThreads) potential_kernel(long long n, con
 
 int potential_blocks(long long n) { return (int)((n + kPotThreads - 1) / kPotThreads); }
 
-void launch_potential(long long n, const Particles& P, bool split, double eps2, double* partial, cudaStream_t s) {
-    potential_kernel<<<potential_blocks(n), kPotThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, eps2, partial);
+void launch_potential(long long n, const Particles& P, bool split, double eps2, double spline_h, double* partial,
+                      cudaStream_t s) {
+    potential_kernel<<<potential_blocks(n), kPotThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, eps2, spline_h,
+                                                                 partial);
 }
 
 // ---------------------------------------------------------------------------
@@ -394,7 +404,7 @@ constexpr int kSampThreads = 256;
 __global__ void __launch_bounds__(kSampThreads) sampler_kernel(long long n, const float4* __restrict__ pos,
                                                                const float4* __restrict__ plo,
                                                                const int* __restrict__ slots, double eps2,
-                                                               double* __restrict__ out) {
+                                                               double spline_h, double* __restrict__ out) {
     __shared__ double red[32];
     const int ti = slots[blockIdx.x];
     const float4 tp = pos[ti];
@@ -412,9 +422,16 @@ __global__ void __launch_bounds__(kSampThreads) sampler_kernel(long long n, cons
             z += (double)l.z;
         }
         const double dx = x - xi, dy = y - yi, dz = z - zi;
-        const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-        const double inv = rsqrt(r2);
-        const double s = (double)p.w * inv * inv * inv;
+        double s;
+        if (spline_h > 0.0) {
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            const double r = sqrt(r2);
+            s = r2 > 0.0 ? (double)p.w * spline_chi_d(r / spline_h) / (r2 * r) : 0.0;
+        } else {
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double inv = rsqrt(r2);
+            s = (double)p.w * inv * inv * inv;
+        }
         ax += s * dx;
         ay += s * dy;
         az += s * dz;
@@ -486,10 +503,11 @@ double run_fma_probe(int sm_count, cudaStream_t s) {
 // (share, target) are reduced in share order by sampler_reduce_kernel.
 constexpr int kSampTile = 256;
 
+template <int SOFT>
 __global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, const float4* __restrict__ pos,
                                                                  const float4* __restrict__ plo,
                                                                  const int* __restrict__ slots, int nslots,
-                                                                 float eps2, long long share,
+                                                                 float eps2, float ih, long long share,
                                                                  double* __restrict__ partial) {
     __shared__ float4 sp[kSampTile];
     __shared__ float4 sl[kSampTile];
@@ -515,9 +533,7 @@ __global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, c
             const float dx = (p.x - tp.x) + (l.x - tl.x);
             const float dy = (p.y - tp.y) + (l.y - tl.y);
             const float dz = (p.z - tp.z) + (l.z - tl.z);
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            const float inv = rsqrtf(r2);
-            const float f = base + k == ti ? 0.f : p.w * inv * inv * inv;
+            const float f = base + k == ti ? 0.f : pair_factor<SOFT>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), p.w, eps2, ih);
             px = fmaf(f, dx, px);
             py = fmaf(f, dy, py);
             pz = fmaf(f, dz, pz);
@@ -553,17 +569,21 @@ int sampler_shares(long long n, int nslots, int sm_count) {
 }
 
 void launch_sampler(long long n, const Particles& P, bool split, const int* slots, int nslots, double eps2,
-                    bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s) {
+                    double spline_h, bool fp64_pairs, double* out, double* partial, int shares, cudaStream_t s) {
     if (nslots <= 0) return;
     if (fp64_pairs) {
-        sampler_kernel<<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, out);
+        sampler_kernel<<<nslots, kSampThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, eps2, spline_h, out);
         return;
     }
     long long share = (n + shares - 1) / shares;
     share = (share + kSampTile - 1) / kSampTile * kSampTile;
     const dim3 grid((nslots + kSampTile - 1) / kSampTile, shares);
-    sampler_tiled_kernel<<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots, (float)eps2,
-                                                    share, partial);
+    if (spline_h > 0.0)
+        sampler_tiled_kernel<kSoftSpline><<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots,
+                                                                    0.f, (float)(1.0 / spline_h), share, partial);
+    else
+        sampler_tiled_kernel<kSoftPlummer><<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots,
+                                                                     (float)eps2, 0.f, share, partial);
     sampler_reduce_kernel<<<(3 * nslots + 255) / 256, 256, 0, s>>>(partial, nslots, shares, out);
 }
 

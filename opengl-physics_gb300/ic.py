@@ -128,6 +128,15 @@ def ensemble_sizes(nsys: int = 512, lo: int = 1024, hi: int = 65536, seed: int =
     return np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), nsys))).astype(np.int64)
 
 
+def ensemble(nsys: int = 512, lo: int = 1024, hi: int = 65536, size_seed: int = 0):
+    """Ensemble of Plummer spheres (system i: seed i, N_i log-uniform in
+    [lo, hi]), concatenated; returns (x, y, z, vx, vy, vz, m), offsets."""
+    sizes = ensemble_sizes(nsys, lo, hi, size_seed)
+    parts = [plummer(int(n), seed=i) for i, n in enumerate(sizes)]
+    arrs = tuple(np.concatenate([p[c] for p in parts]) for c in range(7))
+    return arrs, np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+
+
 def uniform_ball(n: int, seed: int = 4, radius: float = 1.0, total_mass: float = 1.0):
     """Uniform-density ball by rejection from the cube, at rest."""
     rng = np.random.default_rng(seed)

@@ -303,9 +303,49 @@ void or_tree_free(or_tree* t) {
 /* Force kernels                                                            */
 /* ------------------------------------------------------------------------ */
 
-/* AccumPairPlummer (Solvers.cpp:19-38): a += G m d / (|d|^2 + eps^2)^(3/2). */
+/* Softening kind of every pair force and potential: 0 Plummer, 1 spline
+ * (Softening.hpp:30-33); the spline's smoothing length is h = sqrt(eps2). */
+static int g_soft = 0;
+void or_set_softening(int kind) { g_soft = kind; }
+
+/* SplineChi3D / SplinePotential3D (Softening.hpp:36-56): enclosed-mass
+ * fraction and pair potential (times h / (G m)) of the cubic-spline kernel. */
+static inline double spline_chi(double q) {
+    if (q >= 2.0) return 1.0;
+    if (q < 1.0) return q * q * q * (4.0 / 3.0 - 1.2 * q * q + 0.5 * q * q * q);
+    const double t = 2.0 - q, t2 = t * t, t4 = t2 * t2;
+    return 1.0 - 4.0 * (t4 / 4.0 - t4 * t / 5.0 + t4 * t2 / 24.0);
+}
+
+static inline double spline_phi(double q) {
+    if (q >= 2.0) return -1.0 / q;
+    if (q < 1.0) return -(1.4 - (2.0 / 3.0) * q * q + 0.3 * q * q * q * q - 0.1 * q * q * q * q * q);
+    const double t = 2.0 - q, t2 = t * t, t4 = t2 * t2;
+    const double F = t4 / 4.0 - t4 * t / 5.0 + t4 * t2 / 24.0;
+    return -((1.0 - 4.0 * F) / q + t4 / 2.0 - t4 * t / 5.0);
+}
+
+/* AccumPairSpline (Solvers.cpp:43-63): a += G m chi(r/h) d / r^3, nothing
+ * for coincident points. */
+static inline void accum_pair_spline(double dx, double dy, double dz, double gm, double h, double* ax, double* ay,
+                                     double* az) {
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double r = sqrt(r2);
+    if (r <= 1e-300) return;
+    const double s = gm * spline_chi(r / h) / (r2 * r);
+    *ax += s * dx;
+    *ay += s * dy;
+    *az += s * dz;
+}
+
+/* AccumPairPlummer (Solvers.cpp:19-38): a += G m d / (|d|^2 + eps^2)^(3/2);
+ * the spline pair when g_soft selects it (AccumPair, :65-73). */
 static inline void accum_pair(double dx, double dy, double dz, double gm, double eps2, double* ax, double* ay,
                               double* az) {
+    if (g_soft == 1) {
+        accum_pair_spline(dx, dy, dz, gm, sqrt(eps2), ax, ay, az);
+        return;
+    }
     const double dist2 = dx * dx + dy * dy + dz * dz + eps2;
     const double inv = 1.0 / sqrt(dist2);
     const double inv3 = inv * inv * inv;
@@ -652,8 +692,14 @@ void or_diagnostics(int n, const double* x, const double* y, const double* z, co
         double local = 0.0;
         for (int j = i + 1; j < n; ++j) {
             const double dx = x[j] - x[i], dy = y[j] - y[i], dz = z[j] - z[i];
-            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            local -= G * m[i] * m[j] / sqrt(r2);
+            if (g_soft == 1) { /* System.hpp:140-147 */
+                const double r = sqrt(dx * dx + dy * dy + dz * dz);
+                const double q = r <= 1e-300 ? 0.0 : r / eps;
+                local += G * m[i] * m[j] * spline_phi(q) / eps;
+            } else {
+                const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                local -= G * m[i] * m[j] / sqrt(r2);
+            }
         }
         potential += local;
     }

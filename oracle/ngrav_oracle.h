@@ -53,6 +53,10 @@ typedef struct or_counters {
     long long groups;      /* leaf groups walked */
 } or_counters;
 
+/* Softening of every pair force and potential after this call: 0 Plummer,
+ * 1 the cubic spline with h = eps (Softening.hpp:30-33).  Process-wide. */
+void or_set_softening(int kind);
+
 /* Tree build: Tree.cpp:33-52 (ctor), :54-88 (BuildRoot), :90-145
  * (NewChild/Insert/InsertIntoChild), :147-203 (Finalize).  Returns 0 on
  * success, -1 on allocation failure. */

@@ -105,10 +105,16 @@ class _Common:
         return out
 
 
+def _set_softening(self, kind):
+    """0: Plummer, 1: cubic spline with h = eps, for every later call."""
+    self.lib.or_set_softening(int(kind))
+
+
 class Oracle(_Common):
     """The C restatement (oracle/ngrav_oracle.c)."""
 
     _prefix = "or_"
+    set_softening = _set_softening
 
     def __init__(self, path: str = ORACLE_SO):
         if not os.path.isfile(path):
@@ -246,6 +252,10 @@ class Reference(_Common):
 
     def _direct(self, n, x, y, z, m, G, eps, ax, ay, az):
         self.lib.ref_direct_accel(n, _dp(x), _dp(y), _dp(z), _dp(m), G, eps, _dp(ax), _dp(ay), _dp(az))
+
+    def set_softening(self, kind):
+        """0: Plummer, 1: cubic spline with h = eps, for every later call."""
+        self.lib.ref_set_softening(int(kind))
 
     def plummer(self, n, seed):
         """The reference's own Plummer generator (mt19937; clips r at 20)."""

@@ -50,10 +50,12 @@ SoA<3> MakeSoA(int n, const double* x, const double* y, const double* z, const d
     return s;
 }
 
+int g_soft_kind = 0;  // 0 Plummer, 1 spline (ref_set_softening)
+
 StepParams MakeParams(double G, double eps, double theta) {
     StepParams sp;
     sp.G = G;
-    sp.soft = Softening::Plummer(eps);
+    sp.soft = g_soft_kind == 1 ? Softening::Spline(eps) : Softening::Plummer(eps);
     sp.mac.theta = theta;
     sp.mac.kind = MacKind::Geometric;
     sp.solver = Solver::BarnesHut;
@@ -67,6 +69,10 @@ struct TreeHandle {
 } // namespace
 
 extern "C" {
+
+// Softening kind of every later call: 0 Plummer, 1 spline (Softening.hpp:125-139).
+void ref_set_softening(int kind) { g_soft_kind = kind; }
+
 
 int ref_plummer(int n, unsigned seed, double* x, double* y, double* z, double* vx, double* vy, double* vz,
                 double* m) {

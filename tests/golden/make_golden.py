@@ -11,6 +11,7 @@ so the GPU state (FP32 / double-float) holds exactly the same inputs.
 
     python tests/golden/make_golden.py              # every fixture
     python tests/golden/make_golden.py scenarios    # scenarios.npz only
+    python tests/golden/make_golden.py spline       # spline4k.npz only
 """
 from __future__ import annotations
 
@@ -61,14 +62,40 @@ def make_scenarios(R):
     np.savez_compressed(os.path.join(HERE, "scenarios.npz"), **d)
 
 
+def make_spline(R, ic):
+    """Cubic-spline softening (Softening.hpp:30-56): Plummer 4,096 (seed 11),
+    h = 0.02, leaf capacity 16, theta 0.5, 10 KDK steps of 1e-3."""
+    n, ncrit, G, h, theta, dt, steps = 4096, 16, 1.0, 0.02, 0.5, 1e-3, 10
+    x, y, z, vx, vy, vz, m = (f32(a) for a in ic.plummer(n, seed=11))
+    R.set_softening(1)
+    try:
+        d = dict(x=x, y=y, z=z, vx=vx, vy=vy, vz=vz, m=m, G=G, eps=h, theta=theta, ncrit=ncrit, dt=dt, steps=steps)
+        ax, ay, az = R.bh_accel(x, y, z, m, G, h, theta, ncrit)
+        d.update(ax=ax, ay=ay, az=az)
+        dx, dy, dz = R.direct(x, y, z, m, G, h)
+        d.update(dax=dx, day=dy, daz=dz)
+        (sx, sy, sz, svx, svy, svz), _ = R.leapfrog((x, y, z, vx, vy, vz), m, G, h, theta, ncrit, dt, steps)
+        d.update(kdk_x=sx, kdk_y=sy, kdk_z=sz, kdk_vx=svx, kdk_vy=svy, kdk_vz=svz)
+        d["diag0"] = R.diagnostics(x, y, z, vx, vy, vz, m, G, h)
+        d["diag10"] = R.diagnostics(sx, sy, sz, svx, svy, svz, m, G, h)
+    finally:
+        R.set_softening(0)
+    np.savez_compressed(os.path.join(HERE, "spline4k.npz"), **d)
+
+
 def main():
     orc = ge.load_oracle()
     if orc.build_reference() is None:
         raise SystemExit("reference sources not found; set NGRAV_REFERENCE")
     R = orc.Reference()
+    pkg_ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
+    if sys.argv[1:] == ["spline"]:
+        make_spline(R, pkg_ic)
+        return
     make_scenarios(R)
     if sys.argv[1:] == ["scenarios"]:
         return
+    make_spline(R, pkg_ic)
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
 
     # 1) Plummer N=16,384, seed 0: leaf capacity 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK steps.
