@@ -55,8 +55,12 @@ enum {
  * (exactly Newtonian beyond 2 eps). */
 enum { NGRAV_SOFTENING_PLUMMER = 0, NGRAV_SOFTENING_SPLINE = 1 };
 
-/* Multipole acceptance criterion (include/ngrav/Mac.hpp:8-11). */
-enum { NGRAV_MAC_GEOMETRIC = 0, NGRAV_MAC_LEARNED = 1 };
+/* Multipole acceptance criterion (include/ngrav/Mac.hpp:8-11).  GEOMETRIC:
+ * the grouped walk with the group opening test; RELATIVE: the per-particle
+ * walk with the GADGET-2 test M s^2 < alpha |a_old| d^4 / G (geometric for a
+ * particle without a previous |a|), alpha from ngrav_gpu_set_mac_alpha;
+ * LEARNED: the grouped walk with the learned test (below). */
+enum { NGRAV_MAC_GEOMETRIC = 0, NGRAV_MAC_LEARNED = 1, NGRAV_MAC_RELATIVE = 2 };
 
 /* Precision of the particle state and of the force sums.
  * PLAIN: FP32 absolute positions, plain FP32 accumulation.
@@ -161,6 +165,20 @@ int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, cons
 /* FP32 variant: no conversion, for large N. */
 int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
                                 const float* vx, const float* vy, const float* vz, const float* m);
+
+/* One coarse step of length dt with power-of-two rung timesteps
+ * (System::BlockStep, include/ngrav/System.hpp:239-294): each particle's rung
+ * k = min(max_rung, ceil(log2(dt / tau))), tau = eta sqrt(eps / |a|), from its
+ * current acceleration; KDK per rung over 2^rung_max finest substeps, the
+ * force refreshed after every substep for the particles whose step ends there
+ * (geometric per-particle walk, ComputeAccelBarnesHutTargets) on a tree
+ * rebuilt from the drifted positions.  Every particle ends the step with a
+ * fresh acceleration.  rung_max: the largest rung used. */
+int ngrav_gpu_block_step(ngrav_gpu_ctx* ctx, double dt, double eta, int max_rung, int* rung_max);
+
+/* MacParams::alpha of the relative test (include/ngrav/Mac.hpp:18-22;
+ * default 0.001). */
+int ngrav_gpu_set_mac_alpha(ngrav_gpu_ctx* ctx, double alpha);
 
 /* Softening of every pair force, far-field monopole and potential
  * (Softening::Plummer / Softening::Spline, include/ngrav/Softening.hpp:120-140);

@@ -31,7 +31,7 @@ ABI_VERSION = 1
 OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "no particles", 4: "capacity", 5: "non-finite input",
           6: "out of memory", 7: "timeout", 8: "depth limit"}
-MAC_GEOMETRIC, MAC_LEARNED = 0, 1
+MAC_GEOMETRIC, MAC_LEARNED, MAC_RELATIVE = 0, 1, 2
 SOFTENING_PLUMMER, SOFTENING_SPLINE = 0, 1
 PRECISION_PLAIN, PRECISION_SPLIT = 0, 1
 
@@ -39,7 +39,8 @@ PRECISION_PLAIN, PRECISION_SPLIT = 0, 1
 EXPORTS = (
     "ngrav_gpu_default_opts", "ngrav_gpu_create", "ngrav_gpu_destroy", "ngrav_gpu_last_error",
     "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
-    "ngrav_gpu_set_state", "ngrav_gpu_set_state_f32", "ngrav_gpu_set_softening",
+    "ngrav_gpu_set_state", "ngrav_gpu_set_state_f32", "ngrav_gpu_set_softening", "ngrav_gpu_set_mac_alpha",
+    "ngrav_gpu_block_step",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
@@ -180,6 +181,9 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_compute_accel.argtypes = [ctypes.c_void_p, _D, _D, _D]
     L.ngrav_gpu_set_state.argtypes = [ctypes.c_void_p] + [_D] * 6
     L.ngrav_gpu_set_softening.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.ngrav_gpu_set_mac_alpha.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    L.ngrav_gpu_block_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]
     L.ngrav_gpu_set_state_f32.argtypes = [ctypes.c_void_p] + [_F] * 6
     L.ngrav_gpu_prime.argtypes = [ctypes.c_void_p]
     L.ngrav_gpu_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
@@ -335,6 +339,17 @@ class NBodySystem:
     def set_softening(self, kind):
         """SOFTENING_PLUMMER or SOFTENING_SPLINE (h = eps)."""
         self._check(self.L.ngrav_gpu_set_softening(self.h, int(kind)), self.h)
+
+    def block_step(self, dt, eta=0.025, max_rung=8):
+        """One coarse step with power-of-two rung timesteps; returns the largest rung used."""
+        r = ctypes.c_int()
+        self._check(self.L.ngrav_gpu_block_step(self.h, float(dt), float(eta), int(max_rung), ctypes.byref(r)),
+                    self.h)
+        return r.value
+
+    def set_mac_alpha(self, alpha):
+        """MacParams::alpha of the relative opening test."""
+        self._check(self.L.ngrav_gpu_set_mac_alpha(self.h, float(alpha)), self.h)
 
     def set_state(self, x, y, z, vx=None, vy=None, vz=None):
         """New positions / velocities of the current particles (masses and the

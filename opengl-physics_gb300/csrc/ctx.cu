@@ -44,7 +44,7 @@ int check_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* o) {
         return fail(ctx, NGRAV_ERR_INVALID_ARG, "theta/eps/G invalid");
     if (o->precision != NGRAV_PRECISION_PLAIN && o->precision != NGRAV_PRECISION_SPLIT)
         return fail(ctx, NGRAV_ERR_INVALID_ARG, "unknown precision");
-    if (o->mac != NGRAV_MAC_GEOMETRIC && o->mac != NGRAV_MAC_LEARNED)
+    if (o->mac != NGRAV_MAC_GEOMETRIC && o->mac != NGRAV_MAC_LEARNED && o->mac != NGRAV_MAC_RELATIVE)
         return fail(ctx, NGRAV_ERR_INVALID_ARG, "unknown mac");
     return NGRAV_OK;
 }
@@ -231,6 +231,17 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     rec(ctx, 4);
     WalkParams wp = walk_params(ctx, kick, hdt);
     const void* model = nullptr;
+    if (ctx->block_on || ctx->opts.mac == NGRAV_MAC_RELATIVE) {
+        // per-particle walk: decisions, sums and the closing kick in one
+        // kernel; block timesteps take the geometric test on their targets
+        // (ComputeAccelBarnesHutTargets, Solvers.cpp:384-405)
+        rec(ctx, 5);
+        launch_walk_pp(ctx->T, ctx->C, P, ctx->leaf_list, wp, ctx->block_on ? 0 : 1, ctx->alpha, nullptr,
+                       ctx->block_on ? ctx->block_args : nullptr, ctx->block_base, ctx->LB.nwarps, s);
+        rec(ctx, 6);
+        ctx->launches += 1;
+        return;
+    }
     if (lmac_walk_setup(ctx, wp, &model))
         lmac_launch_walk(ctx, wp, model);
     else
@@ -416,6 +427,7 @@ std::vector<unsigned char> step_key(const ngrav_gpu_ctx* ctx, float hdt, float f
     put(&ctx->F, sizeof(ctx->F));
     put(&ctx->walk_stack, sizeof(ctx->walk_stack));
     put(&ctx->soft, sizeof(ctx->soft));
+    put(&ctx->alpha, sizeof(ctx->alpha));
     put(&ctx->p2p_tile, sizeof(ctx->p2p_tile));
     put(&ctx->events, sizeof(ctx->events));
     put(&hdt, sizeof(hdt));
@@ -646,6 +658,52 @@ int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, c
     return set_particles_impl<float>(ctx, n, x, y, z, vx, vy, vz, m, false);
 }
 
+
+int ngrav_gpu_block_step(ngrav_gpu_ctx* ctx, double dt, double eta, int max_rung, int* rung_max) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!(dt > 0.0) || !(eta > 0.0) || max_rung < 0 || max_rung > 20)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "bad dt / eta / max_rung");
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    if (!ctx->primed) NG_TRY(ngrav_gpu_prime(ctx));
+    NG_TRY(ensure_partial(ctx, 2));
+    int* drmax = reinterpret_cast<int*>(ctx->dpartial);
+    NG_CUDA(cudaMemsetAsync(drmax, 0, sizeof(int), ctx->stream));
+    launch_rungs(ctx->n, ctx->P, dt, eta, ctx->opts.eps, max_rung, drmax, ctx->stream);
+    int rmax = 0;
+    NG_CUDA(cudaMemcpyAsync(&rmax, drmax, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->launches += 1;
+    const int nsub = 1 << rmax;
+    const float dtmin = (float)(dt / nsub);
+    NG_CUDA(cudaEventRecord(ctx->sev[0], ctx->stream));
+    int rc = NGRAV_OK;
+    for (int sub = 0; sub < nsub && rc == NGRAV_OK; ++sub) {
+        launch_block_kick_drift(ctx->n, ctx->P, split_of(ctx), dt, sub, rmax, dtmin, ctx->stream);
+        ctx->launches += 1;
+        ctx->block_on = true;
+        ctx->block_args[0] = sub;
+        ctx->block_args[1] = rmax;
+        ctx->block_base = dt;
+        rc = evaluate(ctx, false, true, 0.f);
+        ctx->block_on = false;
+    }
+    NG_TRY(rc);
+    NG_CUDA(cudaEventRecord(ctx->sev[1], ctx->stream));
+    NG_CUDA(cudaEventSynchronize(ctx->sev[1]));
+    float ms = 0.f;
+    NG_CUDA(cudaEventElapsedTime(&ms, ctx->sev[0], ctx->sev[1]));
+    ctx->cum_ms_step += ms;
+    if (rung_max) *rung_max = rmax;
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_set_mac_alpha(ngrav_gpu_ctx* ctx, double alpha) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!(alpha > 0.0) || !std::isfinite(alpha)) return fail(ctx, NGRAV_ERR_INVALID_ARG, "alpha must be positive");
+    ctx->alpha = alpha;
+    return NGRAV_OK;
+}
 
 int ngrav_gpu_set_softening(ngrav_gpu_ctx* ctx, int kind) {
     if (!ctx) return NGRAV_ERR_INVALID_ARG;

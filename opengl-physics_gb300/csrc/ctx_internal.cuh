@@ -60,6 +60,11 @@ struct ngrav_gpu_ctx {
     int walk_stack = 2048;            // tuned: per-warp shared-memory walk stack entries
     int p2p_tile = 0;                 // tuned: sources per near batch (0: the kernel's maximum)
     int soft = 0;                     // kSoftPlummer / kSoftSpline (softening.cuh)
+    double alpha = 0.001;             // relative opening test tolerance
+    // block-timestep evaluation in progress: {finest substep, max rung}
+    bool block_on = false;
+    int block_args[2] = {0, 0};
+    double block_base = 0.0;
     // ensemble of independent systems (Forest of engine.cuh); nsys = 1: one system
     Forest F;
     long long* f_off = nullptr;

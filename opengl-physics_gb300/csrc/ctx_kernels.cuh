@@ -49,4 +49,16 @@ void launch_forest_diag(const Particles& P, bool split, const Forest& F, double*
 void launch_forest_potential(const Particles& P, bool split, const Forest& F, double eps2, int chunks, double* part,
                              cudaStream_t s);
 
+// walk_pp.cu: the per-particle walk (relative MAC, target subsets), with the
+// force sums and the closing kick.
+// block = {sub, rmax}: block-timestep mode (nullptr: every particle).
+void launch_walk_pp(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, const WalkParams& wp,
+                    int relative, double alpha, const unsigned char* targets, const int* block, double block_base,
+                    int nwarps, cudaStream_t s);
+// kdk.cu: block timesteps
+void launch_rungs(long long n, const Particles& P, double base, double eta, double eps, int max_rung, int* rmax,
+                  cudaStream_t s);
+void launch_block_kick_drift(long long n, const Particles& P, bool split, double base, int sub, int rmax, float dtmin,
+                             cudaStream_t s);
+
 }  // namespace ngrav

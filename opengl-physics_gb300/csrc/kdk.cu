@@ -396,6 +396,95 @@ void launch_potential(long long n, const Particles& P, bool split, double eps2, 
 }
 
 // ---------------------------------------------------------------------------
+// Block (power-of-two rung) timesteps, System::BlockStep (System.hpp:239-294):
+// rung_k = min(max_rung, ceil(log2(dt / tau))) with tau = eta sqrt(eps / |a|)
+// (0 when tau >= dt or |a| = 0), stored in vel.w so it travels with the
+// particle through every re-sort; per finest substep the particles whose rung
+// step starts there take their opening half-kick, then everyone drifts.
+// ---------------------------------------------------------------------------
+
+__global__ void rung_kernel(long long n, float4* __restrict__ vel, const float4* __restrict__ acc, double base,
+                            double eta, double eps, int max_rung, int* __restrict__ rmax) {
+    int local = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float4 a = acc[i];
+        const double amag = sqrt((double)a.x * a.x + (double)a.y * a.y + (double)a.z * a.z);
+        int k = 0;
+        if (amag > 0.0 && eps > 0.0) {
+            const double tau = eta * sqrt(eps / amag);
+            if (tau < base) {
+                const double r = ceil(log2(base / tau));
+                k = r < (double)max_rung ? (int)r : max_rung;
+            }
+        }
+        float4 v = vel[i];
+        v.w = (float)k;
+        vel[i] = v;
+        local = max(local, k);
+    }
+    for (int o = 16; o > 0; o >>= 1) local = max(local, __shfl_xor_sync(0xffffffffu, local, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(rmax, local);
+}
+
+template <bool SPLIT>
+__global__ void __launch_bounds__(256) block_kick_drift_kernel(long long n, float4* __restrict__ pos,
+                                                               float4* __restrict__ plo, float4* __restrict__ vel,
+                                                               const float4* __restrict__ acc, double base, int sub,
+                                                               int rmax, float dtmin) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 v = vel[i];
+        const int rung = (int)v.w;
+        const int units = 1 << (rmax - rung);
+        if (sub % units == 0) {
+            const float h = (float)(0.5 * base / (double)(1 << rung));
+            const float4 a = acc[i];
+            v.x = fmaf(h, a.x, v.x);
+            v.y = fmaf(h, a.y, v.y);
+            v.z = fmaf(h, a.z, v.z);
+            vel[i] = v;
+        }
+        float4 p = pos[i];
+        if (SPLIT) {
+            float4 l = plo[i];
+            float* ph = &p.x;
+            float* pl = &l.x;
+            const float dv[3] = {dtmin * v.x, dtmin * v.y, dtmin * v.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {  // (hi, lo) += d with an error-free two-sum
+                const float s = ph[k] + dv[k];
+                const float bb = s - ph[k];
+                const float err = (ph[k] - (s - bb)) + (dv[k] - bb);
+                const float lo = pl[k] + err;
+                const float hi2 = s + lo;
+                pl[k] = lo - (hi2 - s);
+                ph[k] = hi2;
+            }
+            plo[i] = l;
+        } else {
+            p.x = fmaf(dtmin, v.x, p.x);
+            p.y = fmaf(dtmin, v.y, p.y);
+            p.z = fmaf(dtmin, v.z, p.z);
+        }
+        pos[i] = p;
+    }
+}
+
+void launch_rungs(long long n, const Particles& P, double base, double eta, double eps, int max_rung, int* rmax,
+                  cudaStream_t s) {
+    rung_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.vel, P.acc, base, eta, eps, max_rung, rmax);
+}
+
+void launch_block_kick_drift(long long n, const Particles& P, bool split, double base, int sub, int rmax, float dtmin,
+                             cudaStream_t s) {
+    if (split)
+        block_kick_drift_kernel<true><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.acc, base,
+                                                                                 sub, rmax, dtmin);
+    else
+        block_kick_drift_kernel<false><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, nullptr, P.vel, P.acc,
+                                                                                  base, sub, rmax, dtmin);
+}
+
+// ---------------------------------------------------------------------------
 // Direct-sum force-error sampler.  FP64 pairs: one block per target slot.
 // ---------------------------------------------------------------------------
 

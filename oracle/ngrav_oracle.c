@@ -512,6 +512,82 @@ int or_bh_accel(int n, const double* x, const double* y, const double* z, const 
     return 0;
 }
 
+/* WalkBH (Solvers.cpp:181-227): the per-particle walk.  Leaves: every member
+ * but the target itself, exactly; internal nodes: accepted by the geometric
+ * test (2h)^2 < theta^2 d^2, or, with the relative MAC and a previous
+ * |a| > 0, by M s^2 < alpha |a_old| d^4 / G (Mac.hpp:31-42); accepted nodes
+ * add the softened monopole and the unsoftened quadrupole. */
+static void walk_pp(const or_tree* t, const double* x, const double* y, const double* z, const double* m, int nd,
+                    int i, double G, double eps2, double theta2, int relative, double alpha, double aold,
+                    double* ax, double* ay, double* az, long long* pairs, long long* p2c, long long* tests) {
+    if (t->mass[nd] <= 0.0) return;
+    if (t->nchild[nd] == 0) {
+        const int lo = t->first[nd], hi = lo + t->count[nd];
+        for (int k = lo; k < hi; ++k) {
+            const int p = t->order[k];
+            if (p == i) continue;
+            accum_pair(x[p] - x[i], y[p] - y[i], z[p] - z[i], G * m[p], eps2, ax, ay, az);
+            ++*pairs;
+        }
+        return;
+    }
+    const double dx = t->comx[nd] - x[i], dy = t->comy[nd] - y[i], dz = t->comz[nd] - z[i];
+    const double dist2 = dx * dx + dy * dy + dz * dz;
+    const double size = 2.0 * t->half[nd];
+    ++*tests;
+    int accept;
+    if (relative && aold > 0.0)
+        accept = (t->mass[nd] * size * size) < (alpha * aold * dist2 * dist2 / G);
+    else
+        accept = (size * size) < (theta2 * dist2);
+    if (accept) {
+        accum_pair(dx, dy, dz, G * t->mass[nd], eps2, ax, ay, az);
+        if (t->has_quad) add_quadrupole(t->q + 5 * nd, dx, dy, dz, dist2, G, ax, ay, az);
+        ++*p2c;
+        return;
+    }
+    for (int c = 0; c < 8; ++c) {
+        const int ch = t->child[8 * nd + c];
+        if (ch != -1)
+            walk_pp(t, x, y, z, m, ch, i, G, eps2, theta2, relative, alpha, aold, ax, ay, az, pairs, p2c, tests);
+    }
+}
+
+/* ComputeAccelBarnesHutPerParticle (Solvers.cpp:359-382); aold may be NULL
+ * (no history: every target takes the geometric test).  targets: NULL for
+ * all particles, else only those i with targets[i] != 0 are computed
+ * (ComputeAccelBarnesHutTargets, :384-405, geometric). */
+int or_bh_pp_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
+                   double theta, int ncrit, int quad, int relative, double alpha, const double* aold,
+                   const unsigned char* targets, double* ax, double* ay, double* az, or_counters* cnt) {
+    or_tree t;
+    if (or_tree_build(&t, n, x, y, z, m, ncrit, 40)) {
+        or_tree_free(&t);
+        return -1;
+    }
+    if (quad) or_tree_quadrupoles(&t, x, y, z, m);
+    long long pairs = 0, p2c = 0, tests = 0;
+    const double eps2 = eps * eps, theta2 = theta * theta;
+#pragma omp parallel for reduction(+ : pairs, p2c, tests) schedule(dynamic, 64) if (n > 256)
+    for (int i = 0; i < n; ++i) {
+        if (targets && !targets[i]) continue;
+        double axi = 0.0, ayi = 0.0, azi = 0.0;
+        walk_pp(&t, x, y, z, m, 0, i, G, eps2, theta2, relative, alpha, aold ? aold[i] : 0.0, &axi, &ayi, &azi, &pairs,
+                &p2c, &tests);
+        ax[i] = axi;
+        ay[i] = ayi;
+        az[i] = azi;
+    }
+    if (cnt) {
+        cnt->p2p_pairs = pairs;
+        cnt->p2c_terms = p2c;
+        cnt->mac_tests = tests;
+        cnt->groups = 0;
+    }
+    or_tree_free(&t);
+    return 0;
+}
+
 #include <time.h>
 
 static double now_ms(void) {

@@ -77,6 +77,11 @@ void or_bh_group(const or_tree* t, const double* x, const double* y, const doubl
 /* Convenience: tree (ncrit) + quadrupoles (if quad) + grouped walk, the
  * body of the Barnes-Hut branch of System::ComputeAccel
  * (include/ngrav/System.hpp:57-66).  Returns 0 on success. */
+/* Solvers.cpp:181-227, :359-405: per-particle walk, geometric or relative
+ * MAC (aold: previous |a| per particle, NULL = none), optional target subset. */
+int or_bh_pp_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
+                   double theta, int ncrit, int quad, int relative, double alpha, const double* aold,
+                   const unsigned char* targets, double* ax, double* ay, double* az, or_counters* cnt);
 int or_bh_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
                 double theta, int ncrit, int quad, double* ax, double* ay, double* az, or_counters* cnt);
 

@@ -188,6 +188,25 @@ class Oracle(_Common):
                                    _dp(ay), _dp(az))
         return ax, ay, az
 
+    def bh_pp_accel(self, x, y, z, m, G, eps, theta, ncrit=8, quad=True, relative=False, alpha=0.001, aold=None,
+                    targets=None, counters=False):
+        """Per-particle walk (WalkBH): geometric or relative MAC; targets = bool mask."""
+        x, y, z, m = map(_f64, (x, y, z, m))
+        n = len(x)
+        ax, ay, az = np.zeros(n), np.zeros(n), np.zeros(n)
+        ao = None if aold is None else _f64(aold)
+        tg = None if targets is None else np.ascontiguousarray(targets, dtype=np.uint8)
+        cnt = np.zeros(4, np.int64)
+        fn = self.lib.or_bh_pp_accel
+        fn.restype = ctypes.c_int
+        rc = fn(n, _dp(x), _dp(y), _dp(z), _dp(m), ctypes.c_double(G), ctypes.c_double(eps), ctypes.c_double(theta),
+                ncrit, int(quad), int(relative), ctypes.c_double(alpha), None if ao is None else _dp(ao),
+                None if tg is None else tg.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), _dp(ax), _dp(ay), _dp(az),
+                cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)))
+        if rc:
+            raise RuntimeError("or_bh_pp_accel failed")
+        return (ax, ay, az, cnt) if counters else (ax, ay, az)
+
     def leapfrog(self, state, m, G, eps, theta, ncrit, dt, nsteps, acc=None):
         """KDK steps; state = (x, y, z, vx, vy, vz); returns (state, acc)."""
         st = [np.array(a, dtype=np.float64) for a in state]
@@ -256,6 +275,20 @@ class Reference(_Common):
     def set_softening(self, kind):
         """0: Plummer, 1: cubic spline with h = eps, for every later call."""
         self.lib.ref_set_softening(int(kind))
+
+    def bh_pp_accel(self, x, y, z, m, G, eps, theta, ncrit=8, alpha=0.001, aold=None, targets=None):
+        """The reference's relative-MAC walk (aold given) or geometric target walk (targets given)."""
+        x, y, z, m = map(_f64, (x, y, z, m))
+        n = len(x)
+        ax, ay, az = np.zeros(n), np.zeros(n), np.zeros(n)
+        ao = np.zeros(n) if aold is None else _f64(aold)
+        tg = None if targets is None else np.ascontiguousarray(targets, dtype=np.uint8)
+        fn = self.lib.ref_bh_pp_accel
+        fn.restype = None
+        fn(n, _dp(x), _dp(y), _dp(z), _dp(m), ctypes.c_double(G), ctypes.c_double(eps), ctypes.c_double(theta), ncrit,
+           ctypes.c_double(alpha), _dp(ao), None if tg is None else tg.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)),
+           _dp(ax), _dp(ay), _dp(az))
+        return ax, ay, az
 
     def plummer(self, n, seed):
         """The reference's own Plummer generator (mt19937; clips r at 20)."""

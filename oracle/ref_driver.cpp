@@ -12,6 +12,8 @@
 //   ref_direct_accel    -> ngrav::ComputeAccelDirect<3>      (src/Solvers.cpp:77-106)
 //   ref_bh_accel        -> AdaptiveTree<3>(v, ncrit) + ComputeQuadrupoles + ComputeAccelBarnesHut<3>
 //                          (src/Tree.cpp:33-52,205-254; src/Solvers.cpp:407-415)
+//   ref_bh_pp_accel     -> the per-particle walk: relative MAC (src/Solvers.cpp:359-382) or
+//                          geometric on a target subset (:384-405)
 //   ref_tree_*          -> AdaptiveTree<3> node arrays      (include/ngrav/Tree.hpp:44-63)
 //   ref_leapfrog        -> ngrav::LeapfrogStep<3>           (src/Integrator.cpp:9-39)
 //   ref_scenario        -> ngrav::BuildScenario<3>(ScenarioFromString(type), params)
@@ -148,6 +150,36 @@ double ref_bh_accel(int n, const double* x, const double* y, const double* z, co
     std::memcpy(ay, out.ay.data(), sizeof(double) * n);
     std::memcpy(az, out.az.data(), sizeof(double) * n);
     return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+// The relative-MAC walk: ComputeAccelBarnesHut with MacKind::Relative and the
+// previous |a| per particle (Solvers.cpp:407-415 -> :359-382), or, with
+// targets != NULL, the geometric per-particle walk on the particles whose
+// flag is set (ComputeAccelBarnesHutTargets, :384-405).
+void ref_bh_pp_accel(int n, const double* x, const double* y, const double* z, const double* m, double G,
+                     double eps, double theta, int ncrit, double alpha, const double* aold,
+                     const unsigned char* targets, double* ax, double* ay, double* az) {
+    const SoA<3> s = MakeSoA(n, x, y, z, m);
+    const PosMassView<3> v = ViewOf(s);
+    StepParams sp = MakeParams(G, eps, theta);
+    sp.mac.kind = MacKind::Relative;
+    sp.mac.alpha = alpha;
+    AdaptiveTree<3> tree(v, ncrit);
+    tree.ComputeQuadrupoles(v);
+    SoA<3> out;
+    out.ResizeAccel(static_cast<std::size_t>(n));
+    if (targets) {
+        std::vector<int> tg;
+        for (int i = 0; i < n; ++i)
+            if (targets[i]) tg.push_back(i);
+        ComputeAccelBarnesHutTargets<3>(v, MakeParams(G, eps, theta), tree, tg, out);
+    } else {
+        std::vector<double> a(aold, aold + n);
+        ComputeAccelBarnesHut<3>(v, sp, tree, a, out);
+    }
+    std::memcpy(ax, out.ax.data(), sizeof(double) * n);
+    std::memcpy(ay, out.ay.data(), sizeof(double) * n);
+    std::memcpy(az, out.az.data(), sizeof(double) * n);
 }
 
 void* ref_tree_build(int n, const double* x, const double* y, const double* z, const double* m, int ncrit,

@@ -12,6 +12,7 @@ so the GPU state (FP32 / double-float) holds exactly the same inputs.
     python tests/golden/make_golden.py              # every fixture
     python tests/golden/make_golden.py scenarios    # scenarios.npz only
     python tests/golden/make_golden.py spline       # spline4k.npz only
+    python tests/golden/make_golden.py pp           # pp4k.npz only
 """
 from __future__ import annotations
 
@@ -83,6 +84,22 @@ def make_spline(R, ic):
     np.savez_compressed(os.path.join(HERE, "spline4k.npz"), **d)
 
 
+def make_pp(R, ic):
+    """The per-particle walk: relative MAC (alpha 1e-3, previous |a| = the
+    direct-sum |a|) and the geometric walk on every third particle; Plummer
+    4,096 (seed 13), eps 0.02, leaf capacity 8, theta 0.5."""
+    n, ncrit, G, eps, theta, alpha = 4096, 8, 1.0, 0.02, 0.5, 1e-3
+    x, y, z, vx, vy, vz, m = (f32(a) for a in ic.plummer(n, seed=13))
+    dx, dy, dz = R.direct(x, y, z, m, G, eps)
+    aold = np.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
+    rx, ry, rz = R.bh_pp_accel(x, y, z, m, G, eps, theta, ncrit, alpha=alpha, aold=aold)
+    tg = (np.arange(n) % 3 == 0).astype(np.uint8)
+    gx, gy, gz = R.bh_pp_accel(x, y, z, m, G, eps, theta, ncrit, targets=tg)
+    np.savez_compressed(os.path.join(HERE, "pp4k.npz"), x=x, y=y, z=z, m=m, G=G, eps=eps, theta=theta, ncrit=ncrit,
+                        alpha=alpha, aold=aold, rel_ax=rx, rel_ay=ry, rel_az=rz, targets=tg, tgt_ax=gx, tgt_ay=gy,
+                        tgt_az=gz, dax=dx, day=dy, daz=dz)
+
+
 def main():
     orc = ge.load_oracle()
     if orc.build_reference() is None:
@@ -92,10 +109,14 @@ def main():
     if sys.argv[1:] == ["spline"]:
         make_spline(R, pkg_ic)
         return
+    if sys.argv[1:] == ["pp"]:
+        make_pp(R, pkg_ic)
+        return
     make_scenarios(R)
     if sys.argv[1:] == ["scenarios"]:
         return
     make_spline(R, pkg_ic)
+    make_pp(R, pkg_ic)
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
 
     # 1) Plummer N=16,384, seed 0: leaf capacity 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK steps.
