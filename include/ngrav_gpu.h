@@ -166,6 +166,12 @@ int ngrav_gpu_set_particles(ngrav_gpu_ctx* ctx, int64_t n, const double* x, cons
 int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
                                 const float* vx, const float* vy, const float* vz, const float* m);
 
+/* ChooseAdaptiveDt (src/Integrator.cpp:41-59): dt = eta min_i sqrt(eps / |a_i|)
+ * from the current accelerations, clamped to [dt_max / 4096, dt_max]; dt_max
+ * when no particle accelerates or eps = 0.  Primes first if needed.  Take the
+ * step with ngrav_gpu_step(ctx, 1, *dt). */
+int ngrav_gpu_adaptive_dt(ngrav_gpu_ctx* ctx, double eta, double dt_max, double* dt);
+
 /* One coarse step of length dt with power-of-two rung timesteps
  * (System::BlockStep, include/ngrav/System.hpp:239-294): each particle's rung
  * k = min(max_rung, ceil(log2(dt / tau))), tau = eta sqrt(eps / |a|), from its
@@ -175,6 +181,10 @@ int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, c
  * rebuilt from the drifted positions.  Every particle ends the step with a
  * fresh acceleration.  rung_max: the largest rung used. */
 int ngrav_gpu_block_step(ngrav_gpu_ctx* ctx, double dt, double eta, int max_rung, int* rung_max);
+
+/* System::Rungs (include/ngrav/System.hpp:203-205): each particle's rung
+ * from the last block step, in input order (all zero before any). */
+int ngrav_gpu_get_rungs(ngrav_gpu_ctx* ctx, int* rung);
 
 /* MacParams::alpha of the relative test (include/ngrav/Mac.hpp:18-22;
  * default 0.001). */

@@ -40,7 +40,7 @@ EXPORTS = (
     "ngrav_gpu_default_opts", "ngrav_gpu_create", "ngrav_gpu_destroy", "ngrav_gpu_last_error",
     "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
     "ngrav_gpu_set_state", "ngrav_gpu_set_state_f32", "ngrav_gpu_set_softening", "ngrav_gpu_set_mac_alpha",
-    "ngrav_gpu_block_step",
+    "ngrav_gpu_block_step", "ngrav_gpu_get_rungs", "ngrav_gpu_adaptive_dt",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
@@ -182,6 +182,9 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_set_state.argtypes = [ctypes.c_void_p] + [_D] * 6
     L.ngrav_gpu_set_softening.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.ngrav_gpu_set_mac_alpha.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    L.ngrav_gpu_adaptive_dt.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_double)]
+    L.ngrav_gpu_get_rungs.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.ngrav_gpu_block_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_int)]
     L.ngrav_gpu_set_state_f32.argtypes = [ctypes.c_void_p] + [_F] * 6
@@ -346,6 +349,18 @@ class NBodySystem:
         self._check(self.L.ngrav_gpu_block_step(self.h, float(dt), float(eta), int(max_rung), ctypes.byref(r)),
                     self.h)
         return r.value
+
+    def adaptive_dt(self, eta, dt_max):
+        """ChooseAdaptiveDt on the current accelerations."""
+        d = ctypes.c_double()
+        self._check(self.L.ngrav_gpu_adaptive_dt(self.h, float(eta), float(dt_max), ctypes.byref(d)), self.h)
+        return d.value
+
+    def rungs(self):
+        """Each particle's rung from the last block step (input order)."""
+        out = np.zeros(self.n, np.int32)
+        self._check(self.L.ngrav_gpu_get_rungs(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), self.h)
+        return out
 
     def set_mac_alpha(self, alpha):
         """MacParams::alpha of the relative opening test."""

@@ -659,6 +659,31 @@ int ngrav_gpu_set_particles_f32(ngrav_gpu_ctx* ctx, int64_t n, const float* x, c
 }
 
 
+int ngrav_gpu_adaptive_dt(ngrav_gpu_ctx* ctx, double eta, double dt_max, double* dt) {
+    if (!ctx || !dt) return NGRAV_ERR_INVALID_ARG;
+    if (!(dt_max > 0.0) || !(eta > 0.0)) return fail(ctx, NGRAV_ERR_INVALID_ARG, "bad eta / dt_max");
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    if (!ctx->primed) NG_TRY(ngrav_gpu_prime(ctx));
+    *dt = dt_max;
+    const double eps = ctx->opts.eps;
+    if (ctx->n == 0 || !(eps > 0.0)) return NGRAV_OK;
+    NG_TRY(ensure_partial(ctx, 1));
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(ctx->dpartial);
+    NG_CUDA(cudaMemsetAsync(d, 0, sizeof(*d), ctx->stream));
+    launch_amax(ctx->n, ctx->P.acc, d, ctx->stream);
+    ctx->launches += 1;
+    unsigned long long bits = 0;
+    NG_CUDA(cudaMemcpyAsync(&bits, d, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double amax;
+    std::memcpy(&amax, &bits, sizeof(amax));
+    if (!(amax > 0.0)) return NGRAV_OK;
+    const double t = eta * std::sqrt(eps / amax);
+    *dt = std::min(std::max(t, dt_max / 4096.0), dt_max);
+    return NGRAV_OK;
+}
+
 int ngrav_gpu_block_step(ngrav_gpu_ctx* ctx, double dt, double eta, int max_rung, int* rung_max) {
     if (!ctx) return NGRAV_ERR_INVALID_ARG;
     if (!(dt > 0.0) || !(eta > 0.0) || max_rung < 0 || max_rung > 20)
@@ -799,6 +824,18 @@ int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, dou
     for (int k = 0; k < 6; ++k)
         if (outs[k])
             NG_CUDA(cudaMemcpyAsync(outs[k], st + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NGRAV_OK;
+}
+
+int ngrav_gpu_get_rungs(ngrav_gpu_ctx* ctx, int* rung) {
+    if (!ctx || !rung) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    int* st = reinterpret_cast<int*>(ctx->stage);
+    launch_rung_download(n, ctx->P.id, ctx->P.vel, st, ctx->stream);
+    NG_CUDA(cudaMemcpyAsync(rung, st, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));
     NG_CUDA(cudaStreamSynchronize(ctx->stream));
     return NGRAV_OK;
 }

@@ -115,6 +115,16 @@ void launch_download(long long n, const int* id, const float4* a, const float4* 
     download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, a, alo, ox, oy, oz);
 }
 
+__global__ void rung_download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ vel,
+                                     int* __restrict__ out) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        out[id[k]] = (int)vel[k].w;
+}
+
+void launch_rung_download(long long n, const int* id, const float4* vel, int* out, cudaStream_t s) {
+    rung_download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, vel, out);
+}
+
 __global__ void inverse_id_kernel(long long n, const int* __restrict__ id, int* __restrict__ inv) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
         inv[id[k]] = (int)k;
@@ -424,6 +434,22 @@ __global__ void rung_kernel(long long n, float4* __restrict__ vel, const float4*
     }
     for (int o = 16; o > 0; o >>= 1) local = max(local, __shfl_xor_sync(0xffffffffu, local, o));
     if ((threadIdx.x & 31) == 0) atomicMax(rmax, local);
+}
+
+// max_i |a_i| as the bit pattern of a non-negative double (which orders
+// like the unsigned integer), for the adaptive step rule.
+__global__ void amax_kernel(long long n, const float4* __restrict__ acc, unsigned long long* __restrict__ out) {
+    double local = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float4 a = acc[i];
+        local = fmax(local, sqrt((double)a.x * a.x + (double)a.y * a.y + (double)a.z * a.z));
+    }
+    for (int o = 16; o > 0; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(local));
+}
+
+void launch_amax(long long n, const float4* acc, unsigned long long* out, cudaStream_t s) {
+    amax_kernel<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(n, acc, out);
 }
 
 template <bool SPLIT>

@@ -4,6 +4,7 @@
 // ("split" | "plain").
 #include "deck_sim.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <stdexcept>
@@ -28,23 +29,30 @@ void DeckSim::Configure(const fw::Deck& deck) {
         m_warnings.push_back(w);
         std::fprintf(stderr, "warning: %s\n", w.c_str());
     };
-    if (deck.GetBool("time.adaptive", false)) warn("time.adaptive is not supported on this path; fixed dt used");
-    if (deck.GetString("time.scheme", "global") == "block")
-        warn("time.scheme = \"block\" is not supported on this path; the global scheme is used");
+    // time.adaptive / time.eta / time.scheme / time.block_max_rung
+    // (DeckSim.cpp:27-35); block timesteps need a solver with a target-subset
+    // form (Direct / Barnes-Hut, System.hpp:93-98), else the adaptive or
+    // global scheme runs.
+    m_adaptive = deck.GetBool("time.adaptive", false);
+    m_eta = deck.GetDouble("time.eta", 0.03);
+    m_blockMaxRung = std::max(0, deck.GetInt("time.block_max_rung", 8));
     m_substepsPerFrame = deck.GetInt("time.substeps_per_frame", 4);
 
     ngrav_gpu_default_opts(&m_opts);
     const std::string kind = deck.GetString("solver.kind", "barnes_hut");
     m_opts.theta = deck.GetDouble("solver.theta", 0.5);
+    const bool bhOrDirect = kind == "direct" || kind == "barnes_hut" || kind == "bh";
     if (kind == "direct") {
         m_opts.theta = 0.0;  // every node opens: the exact pair sum
-    } else if (kind != "barnes_hut" && kind != "bh") {
+    } else if (!bhOrDirect) {
         warn("solver.kind = \"" + kind + "\" runs as Barnes-Hut (the reference also falls back to it)");
     }
-    if (deck.GetString("solver.mac", "geometric") == "relative")
-        warn("solver.mac = \"relative\" is not supported on this path; the geometric MAC is used");
-    if (deck.GetString("softening.kind", "plummer") == "spline")
-        warn("softening.kind = \"spline\" is not supported on this path; Plummer softening is used");
+    m_block = deck.GetString("time.scheme", "global") == "block" && bhOrDirect;
+    // solver.mac / solver.alpha (DeckSim.cpp:41-42): the relative test runs
+    // on the per-particle walk (Barnes-Hut only; direct opens everything).
+    if (kind != "direct" && deck.GetString("solver.mac", "geometric") == "relative") m_opts.mac = NGRAV_MAC_RELATIVE;
+    m_alpha = deck.GetDouble("solver.alpha", 0.001);
+    m_spline = deck.GetString("softening.kind", "plummer") == "spline";  // DeckSim.cpp:61-62
     m_opts.leaf_capacity = deck.GetInt("solver.leaf_capacity", 8);
     m_opts.quadrupole = deck.GetBool("solver.quadrupole", true) ? 1 : 0;
     m_opts.precision = deck.GetString("precision.mode", "split") == "plain" ? NGRAV_PRECISION_PLAIN
@@ -81,6 +89,10 @@ void DeckSim::LoadScenario() {
         Check(ngrav_gpu_create(&m_ctx, &m_opts), "ngrav_gpu_create");
     else
         Check(ngrav_gpu_set_opts(m_ctx, &m_opts), "ngrav_gpu_set_opts");
+    if (m_opts.mac == NGRAV_MAC_RELATIVE) Check(ngrav_gpu_set_mac_alpha(m_ctx, m_alpha), "ngrav_gpu_set_mac_alpha");
+    Check(ngrav_gpu_set_softening(m_ctx, m_spline ? NGRAV_SOFTENING_SPLINE : NGRAV_SOFTENING_PLUMMER),
+          "ngrav_gpu_set_softening");
+    m_rungMax = 0;
     const State& s = sc.state;
     m_n = (long long)s.Count();
     Check(ngrav_gpu_set_particles(m_ctx, m_n, s.x.data(), s.y.data(), s.z.data(), s.vx.data(), s.vy.data(),
@@ -97,7 +109,29 @@ void DeckSim::LoadScenario() {
 
 void DeckSim::Reset() { LoadScenario(); }
 
+// System::Step per substep (System.hpp:89-107): block, else adaptive, else
+// the fixed-dt KDK (batched into one call, replayed as CUDA graphs).
 void DeckSim::Step(int substeps) {
+    if (m_block) {
+        for (int k = 0; k < substeps; ++k) {
+            Check(ngrav_gpu_block_step(m_ctx, m_dt, m_eta, m_blockMaxRung, &m_rungMax), "ngrav_gpu_block_step");
+            m_lastDt = m_dt;
+            m_time += m_dt;
+            ++m_step;
+        }
+        return;
+    }
+    if (m_adaptive) {
+        for (int k = 0; k < substeps; ++k) {
+            double dt = m_dt;
+            Check(ngrav_gpu_adaptive_dt(m_ctx, m_eta, m_dt, &dt), "ngrav_gpu_adaptive_dt");
+            Check(ngrav_gpu_step(m_ctx, 1, dt), "ngrav_gpu_step");
+            m_lastDt = dt;
+            m_time += dt;
+            ++m_step;
+        }
+        return;
+    }
     Check(ngrav_gpu_step(m_ctx, substeps, m_dt), "ngrav_gpu_step");
     m_lastDt = m_dt;
     m_time += m_dt * substeps;
@@ -135,7 +169,7 @@ void DeckSim::Snapshot(fw::OutputWriter& writer) {
     writer.WriteScalar("com_y", d.com[1]);
     writer.WriteScalar("com_z", d.com[2]);
     writer.WriteScalar("dt_last", m_lastDt);
-    writer.WriteScalar("rung_max", 0.0);  // global scheme only
+    writer.WriteScalar("rung_max", (double)m_rungMax);  // deepest rung of the last block step
 }
 
 fw::SimInfo DeckSim::Info() const {

@@ -52,6 +52,10 @@ private:
     bool m_deckHasG = false, m_deckHasEps = false, m_deckHasDt = false;
     double m_deckG = 1.0, m_deckEps = 0.05, m_deckDt = 1e-3;
     long long m_n = 0;
+    bool m_adaptive = false, m_block = false, m_spline = false;
+    double m_eta = 0.03, m_alpha = 0.001;
+    int m_blockMaxRung = 8;
+    int m_rungMax = 0;
     std::vector<std::string> m_warnings;
 };
 

@@ -754,6 +754,85 @@ int or_leapfrog(int n, double* x, double* y, double* z, double* vx, double* vy, 
     return 0;
 }
 
+/* One block (power-of-two rung) step: System::BlockStep
+ * (include/ngrav/System.hpp:239-294).  a{x,y,z} hold a(t) on entry (primed)
+ * and a(t + dt) on return; rung[i] receives each particle's rung.  The
+ * refreshes use the geometric per-particle walk on the closing set
+ * (ComputeAccelBarnesHutTargets, Solvers.cpp:384-405) on a tree rebuilt from
+ * the drifted positions.  Returns the largest rung, or -1 on failure. */
+int or_block_step(int n, double* x, double* y, double* z, double* vx, double* vy, double* vz, const double* m,
+                  double* ax, double* ay, double* az, double G, double eps, double theta, int ncrit, double dt,
+                  double eta, int max_rung, int* rung) {
+    if (max_rung < 0) max_rung = 0;
+    int rmax = 0;
+    for (int i = 0; i < n; ++i) { /* System.hpp:250-262 */
+        const double amag = sqrt(ax[i] * ax[i] + ay[i] * ay[i] + az[i] * az[i]);
+        int k = 0;
+        if (amag > 0.0 && eps > 0.0) {
+            const double tau = eta * sqrt(eps / amag);
+            if (tau < dt) {
+                k = (int)ceil(log2(dt / tau));
+                if (k > max_rung) k = max_rung;
+            }
+        }
+        rung[i] = k;
+        if (k > rmax) rmax = k;
+    }
+    const int nsub = 1 << rmax;
+    const double dtmin = dt / nsub;
+    unsigned char* act = (unsigned char*)malloc((size_t)(n > 0 ? n : 1));
+    double* bx = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * 3);
+    if (!act || !bx) {
+        free(act);
+        free(bx);
+        return -1;
+    }
+    double* by = bx + n;
+    double* bz = by + n;
+    for (int sub = 0; sub < nsub; ++sub) {
+        for (int i = 0; i < n; ++i) { /* opening half-kick of the rungs starting here */
+            const int units = 1 << (rmax - rung[i]);
+            if (sub % units == 0) {
+                const double h = 0.5 * (dt / (1 << rung[i]));
+                vx[i] += h * ax[i];
+                vy[i] += h * ay[i];
+                vz[i] += h * az[i];
+            }
+        }
+        for (int i = 0; i < n; ++i) { /* drift everyone by the finest substep */
+            x[i] += dtmin * vx[i];
+            y[i] += dtmin * vy[i];
+            z[i] += dtmin * vz[i];
+        }
+        int nact = 0;
+        for (int i = 0; i < n; ++i) {
+            const int units = 1 << (rmax - rung[i]);
+            act[i] = (unsigned char)((sub + 1) % units == 0);
+            nact += act[i];
+        }
+        if (nact) {
+            if (or_bh_pp_accel(n, x, y, z, m, G, eps, theta, ncrit, 1, 0, 0.0, NULL, act, bx, by, bz, NULL)) {
+                free(act);
+                free(bx);
+                return -1;
+            }
+            for (int i = 0; i < n; ++i) {
+                if (!act[i]) continue;
+                ax[i] = bx[i];
+                ay[i] = by[i];
+                az[i] = bz[i];
+                const double h = 0.5 * (dt / (1 << rung[i]));
+                vx[i] += h * ax[i];
+                vy[i] += h * ay[i];
+                vz[i] += h * az[i];
+            }
+        }
+    }
+    free(act);
+    free(bx);
+    return rmax;
+}
+
 void or_diagnostics(int n, const double* x, const double* y, const double* z, const double* vx, const double* vy,
                     const double* vz, const double* m, double G, double eps, double* out) {
     const double eps2 = eps * eps;

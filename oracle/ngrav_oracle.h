@@ -82,6 +82,10 @@ void or_bh_group(const or_tree* t, const double* x, const double* y, const doubl
 int or_bh_pp_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
                    double theta, int ncrit, int quad, int relative, double alpha, const double* aold,
                    const unsigned char* targets, double* ax, double* ay, double* az, or_counters* cnt);
+/* System::BlockStep (include/ngrav/System.hpp:239-294), one coarse step. */
+int or_block_step(int n, double* x, double* y, double* z, double* vx, double* vy, double* vz, const double* m,
+                  double* ax, double* ay, double* az, double G, double eps, double theta, int ncrit, double dt,
+                  double eta, int max_rung, int* rung);
 int or_bh_accel(int n, const double* x, const double* y, const double* z, const double* m, double G, double eps,
                 double theta, int ncrit, int quad, double* ax, double* ay, double* az, or_counters* cnt);
 

@@ -220,6 +220,21 @@ class Oracle(_Common):
             raise RuntimeError("or_leapfrog failed")
         return tuple(st), tuple(a)
 
+    def block_step(self, state, m, G, eps, theta, ncrit, dt, eta, max_rung, acc):
+        """One block (rung) step from (state, acc); returns (state, acc, rungs, rung_max)."""
+        st = [np.array(a, dtype=np.float64) for a in state]
+        a = [np.array(c, dtype=np.float64) for c in acc]
+        m = _f64(m)
+        rung = np.zeros(len(m), np.int32)
+        fn = self.lib.or_block_step
+        fn.restype = ctypes.c_int
+        rmax = fn(len(m), *[_dp(v) for v in st], _dp(m), *[_dp(v) for v in a], ctypes.c_double(G),
+                  ctypes.c_double(eps), ctypes.c_double(theta), ncrit, ctypes.c_double(dt), ctypes.c_double(eta),
+                  int(max_rung), _ip(rung))
+        if rmax < 0:
+            raise RuntimeError("or_block_step failed")
+        return tuple(st), tuple(a), rung, rmax
+
     def force_error(self, x, y, z, m, G, eps, targets, ax, ay, az):
         """(rms, max, median) relative error of (ax, ay, az) vs the FP64 direct sum on targets."""
         x, y, z, m, ax, ay, az = map(_f64, (x, y, z, m, ax, ay, az))
@@ -326,6 +341,20 @@ class Reference(_Common):
         ms = self.lib.ref_bh_accel(n, _dp(x), _dp(y), _dp(z), _dp(m), G, eps, theta, ncrit, int(quad), _dp(ax),
                                    _dp(ay), _dp(az))
         return (ax, ay, az, ms) if timed else (ax, ay, az)
+
+    def block_step(self, state, m, G, eps, theta, dt, eta, max_rung, nsteps=1):
+        """System::Step with StepParams::block, primed from the positions (ncrit 8);
+        returns (state, acc, rungs of the last step)."""
+        st = [np.array(a, dtype=np.float64) for a in state]
+        m = _f64(m)
+        n = len(m)
+        a = [np.zeros(n) for _ in range(3)]
+        rung = np.zeros(n, np.int32)
+        fn = self.lib.ref_block_step
+        fn.restype = None
+        fn(n, *[_dp(v) for v in st], _dp(m), *[_dp(v) for v in a], ctypes.c_double(G), ctypes.c_double(eps),
+           ctypes.c_double(theta), ctypes.c_double(dt), ctypes.c_double(eta), int(max_rung), int(nsteps), _ip(rung))
+        return tuple(st), tuple(a), rung
 
     def leapfrog(self, state, m, G, eps, theta, ncrit, dt, nsteps, acc=None):
         st = [np.array(a, dtype=np.float64) for a in state]

@@ -295,6 +295,44 @@ double ref_leapfrog(int n, double* x, double* y, double* z, double* vx, double* 
     return std::chrono::duration<double, std::milli>(t1 - t0).count();
 }
 
+// nsteps block (power-of-two rung) steps through System::Step with
+// StepParams::block (include/ngrav/System.hpp:89-98 -> BlockStep :239-294),
+// Barnes-Hut, primed by System::Prime from the positions.  The state and a
+// are updated in place; rung[i] receives the rungs of the last step.
+void ref_block_step(int n, double* x, double* y, double* z, double* vx, double* vy, double* vz, const double* m,
+                    double* ax, double* ay, double* az, double G, double eps, double theta, double dt, double eta,
+                    int max_rung, int nsteps, int* rung) {
+    SoA<3> s = MakeSoA(n, x, y, z, m);
+    for (int i = 0; i < n; ++i) {
+        s.vx[i] = vx[i];
+        s.vy[i] = vy[i];
+        s.vz[i] = vz[i];
+    }
+    System<3> sys;
+    sys.SetParticles(std::move(s));
+    StepParams sp = MakeParams(G, eps, theta);
+    sp.dt = dt;
+    sp.block = true;
+    sp.eta = eta;
+    sp.blockMaxRung = max_rung;
+    sys.Prime(sp);
+    for (int k = 0; k < nsteps; ++k) sys.Step(sp);
+    const SoA<3>& st = sys.State();
+    for (int i = 0; i < n; ++i) {
+        x[i] = st.x[i];
+        y[i] = st.y[i];
+        z[i] = st.z[i];
+        vx[i] = st.vx[i];
+        vy[i] = st.vy[i];
+        vz[i] = st.vz[i];
+        ax[i] = st.ax[i];
+        ay[i] = st.ay[i];
+        az[i] = st.az[i];
+    }
+    const std::span<const int> r = sys.Rungs();
+    for (int i = 0; i < n; ++i) rung[i] = i < static_cast<int>(r.size()) ? r[i] : 0;
+}
+
 // out[0] = total energy (O(N^2) potential), out[1..3] = centre of mass,
 // out[4..6] = angular momentum about the COM, out[7..9] = linear momentum.
 void ref_diagnostics(int n, const double* x, const double* y, const double* z, const double* vx, const double* vy,

@@ -100,6 +100,25 @@ def make_pp(R, ic):
                         tgt_az=gz, dax=dx, day=dy, daz=dz)
 
 
+def make_block(R, ic):
+    """Block (power-of-two rung) timesteps, System::Step with
+    StepParams::block: Plummer 4,096 (seed 17), eps 0.01, theta 0.5, coarse
+    dt 0.01, eta 0.025; two steps with max rung 8 (rungs 0-3 in use) and one
+    with max rung 1 (the clamp).  The reference's block path builds its
+    trees with leaf capacity 8."""
+    n, G, eps, theta, dt, eta = 4096, 1.0, 0.01, 0.5, 0.01, 0.025
+    x, y, z, vx, vy, vz, m = (f32(a) for a in ic.plummer(n, seed=17))
+    out = dict(x=x, y=y, z=z, vx=vx, vy=vy, vz=vz, m=m, G=G, eps=eps, theta=theta, dt=dt, eta=eta)
+    for tag, max_rung, steps in (("r8", 8, 2), ("r1", 1, 1)):
+        st, a, rung = R.block_step((x, y, z, vx, vy, vz), m, G, eps, theta, dt, eta, max_rung, nsteps=steps)
+        out.update({f"{tag}_{k}": v for k, v in zip(("x", "y", "z", "vx", "vy", "vz"), st)})
+        out.update({f"{tag}_{k}": v for k, v in zip(("ax", "ay", "az"), a)})
+        out[f"{tag}_rung"] = rung
+        out[f"{tag}_steps"] = steps
+        out[f"{tag}_max_rung"] = max_rung
+    np.savez_compressed(os.path.join(HERE, "block4k.npz"), **out)
+
+
 def main():
     orc = ge.load_oracle()
     if orc.build_reference() is None:
@@ -112,11 +131,15 @@ def main():
     if sys.argv[1:] == ["pp"]:
         make_pp(R, pkg_ic)
         return
+    if sys.argv[1:] == ["block"]:
+        make_block(R, pkg_ic)
+        return
     make_scenarios(R)
     if sys.argv[1:] == ["scenarios"]:
         return
     make_spline(R, pkg_ic)
     make_pp(R, pkg_ic)
+    make_block(R, pkg_ic)
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
 
     # 1) Plummer N=16,384, seed 0: leaf capacity 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK steps.

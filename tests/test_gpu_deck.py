@@ -96,3 +96,109 @@ def test_bench_csv_line(exe):
 def test_selftest_passes(exe):
     r = run(exe, "--selftest")
     assert "selftest: PASS" in r.stdout
+
+
+def ic_deck(tmp_path, ic, n, seed, body, binary=False):
+    x, y, z, vx, vy, vz, m = ic.plummer(n, seed=seed)
+    if binary:  # one heavy tight pair (|a| ~ 30): shrinks the adaptive step / takes deep rungs
+        x[0], y[0], z[0], x[1], y[1], z[1] = 0.02, 0.0, 0.0, -0.02, 0.0, 0.0
+        vx[0], vy[0], vz[0], vx[1], vy[1], vz[1] = 0.0, 0.75, 0.0, 0.0, -0.75, 0.0
+        m[0] = m[1] = 0.05
+    rec = np.stack([x, y, z, m, vx, vy, vz], 1).astype(np.float32)
+    icf = tmp_path / "ic.bin"
+    rec.tofile(icf)
+    deck = tmp_path / "run.toml"
+    deck.write_text(f'title = "deck keys"\n{body}[scenario]\ntype = "ic_file"\nic_file = "{icf}"\n')
+    st = tuple(rec[:, k].astype(np.float64) for k in (0, 1, 2, 4, 5, 6))
+    return deck, st, rec[:, 3].astype(np.float64)
+
+
+def frame(out, f):
+    return (np.load(out / "frames" / f"pos_{f:04d}.npy").astype(np.float64),
+            np.load(out / "frames" / f"vel_{f:04d}.npy").astype(np.float64))
+
+
+def diag_rows(out):
+    with open(out / "diagnostics.csv") as f:
+        return [[float(v) for v in r] for r in list(csv.reader(f))[1:]]
+
+
+def test_deck_block_scheme_follows_oracle(exe, ic, oracle, tmp_path):
+    """time.scheme = "block": each substep is System::BlockStep; frames and
+    the rung_max column follow the oracle's block step."""
+    G, eps, theta, dt, eta, max_rung, frames, sub = 1.0, 0.01, 0.5, 4e-3, 0.03, 6, 3, 2
+    body = (f'[sim]\nG = {G}\n[softening]\neps = {eps}\n[time]\nframes = {frames}\nsubsteps_per_frame = {sub}\n'
+            f'dt = {dt}\nscheme = "block"\nblock_max_rung = {max_rung}\neta = {eta}\n'
+            f'[solver]\nkind = "barnes_hut"\ntheta = {theta}\n')
+    deck, st, mm = ic_deck(tmp_path, ic, 2048, 8, body, binary=True)
+    out = tmp_path / "out"
+    r = run(exe, "--deck", str(deck), "--out", str(out))
+    assert "warning" not in r.stderr
+    rows = diag_rows(out)
+    acc = oracle.bh_accel(*st[0:3], mm, G, eps, theta, 8)
+    for f in range(1, frames):
+        for _ in range(sub):
+            st, acc, rung, rmax = oracle.block_step(st, mm, G, eps, theta, 8, dt, eta, max_rung, acc)
+        pos, vel = frame(out, f)
+        np.testing.assert_allclose(pos, np.stack(st[0:3], 1), rtol=0, atol=5e-6)
+        np.testing.assert_allclose(vel, np.stack(st[3:6], 1), rtol=0, atol=5e-4 * np.abs(st[3]).max())
+        assert rows[f][11] == rmax and rmax >= 3
+        assert rows[f][10] == dt
+
+
+def test_deck_adaptive_dt_follows_oracle(exe, ic, oracle, tmp_path):
+    """time.adaptive: every substep takes ChooseAdaptiveDt of the current
+    accelerations (src/Integrator.cpp:41-59); dt_last reports it."""
+    G, eps, theta, dt, eta, frames, sub = 1.0, 0.01, 0.5, 1e-2, 0.02, 3, 3
+    body = (f'[sim]\nG = {G}\n[softening]\neps = {eps}\n[time]\nframes = {frames}\nsubsteps_per_frame = {sub}\n'
+            f'dt = {dt}\nadaptive = true\neta = {eta}\n[solver]\nkind = "barnes_hut"\ntheta = {theta}\n')
+    deck, st, mm = ic_deck(tmp_path, ic, 2048, 9, body, binary=True)
+    out = tmp_path / "out"
+    r = run(exe, "--deck", str(deck), "--out", str(out))
+    assert "warning" not in r.stderr
+    rows = diag_rows(out)
+    acc = oracle.bh_accel(*st[0:3], mm, G, eps, theta, 8)
+    for f in range(1, frames):
+        for _ in range(sub):
+            a = np.sqrt(acc[0] ** 2 + acc[1] ** 2 + acc[2] ** 2)
+            h = float(np.clip(eta * np.sqrt(eps / a.max()), dt / 4096, dt))
+            st, acc = oracle.leapfrog(st, mm, G, eps, theta, 8, h, 1, acc)
+        assert h < dt
+        assert rows[f][10] == pytest.approx(h, rel=1e-5)
+        assert rows[f][0] == f * sub * dt  # the runner's t is step x nominal dt (HeadlessRunner.cpp:21-23)
+        pos, vel = frame(out, f)
+        np.testing.assert_allclose(pos, np.stack(st[0:3], 1), rtol=0, atol=5e-6)
+
+
+def test_deck_spline_and_relative_mac(exe, ic, oracle, tmp_path):
+    """softening.kind = "spline" follows the oracle's spline leapfrog; and
+    solver.mac = "relative" runs the relative test (no fallback warning),
+    conserving energy."""
+    G, eps, theta, dt, frames, sub = 1.0, 0.05, 0.5, 1e-3, 3, 4
+    body = (f'[sim]\nG = {G}\n[softening]\nkind = "spline"\neps = {eps}\n[time]\nframes = {frames}\n'
+            f'substeps_per_frame = {sub}\ndt = {dt}\n[solver]\nkind = "barnes_hut"\ntheta = {theta}\n')
+    deck, st, mm = ic_deck(tmp_path, ic, 2048, 10, body)
+    out = tmp_path / "out"
+    r = run(exe, "--deck", str(deck), "--out", str(out))
+    assert "warning" not in r.stderr
+    rows = diag_rows(out)
+    oracle.set_softening(1)
+    try:
+        acc = None
+        for f in range(1, frames):
+            st, acc = oracle.leapfrog(st, mm, G, eps, theta, 8, dt, sub, acc)
+            pos, vel = frame(out, f)
+            np.testing.assert_allclose(pos, np.stack(st[0:3], 1), rtol=0, atol=2e-6)
+            d = oracle.diagnostics(*st, mm, G, eps)
+            assert abs(rows[f][2] - d[0]) <= 1e-6 * abs(d[0])
+    finally:
+        oracle.set_softening(0)
+
+    body = (f'[sim]\nG = {G}\n[softening]\neps = {eps}\n[time]\nframes = 4\nsubsteps_per_frame = 5\n'
+            f'dt = {dt}\n[solver]\nkind = "barnes_hut"\nmac = "relative"\nalpha = 0.004\n')
+    deck, _, _ = ic_deck(tmp_path, ic, 2048, 11, body)
+    out = tmp_path / "out_rel"
+    r = run(exe, "--deck", str(deck), "--out", str(out))
+    assert "warning" not in r.stderr
+    rows = diag_rows(out)
+    assert abs(rows[-1][3]) < 0.01  # energy_drift_pct

@@ -120,3 +120,25 @@ def test_oracle_per_particle_walk_matches_reference(oracle):
     # the relative MAC meets its purpose: error well below the geometric walk's at this alpha
     e = rel_err(rx, ry, rz, d["dax"], d["day"], d["daz"])
     assert np.sqrt(np.mean(e ** 2)) < 5e-3
+
+
+def test_oracle_block_step_matches_reference(oracle):
+    """System::BlockStep (System.hpp:239-294): rungs, state and a(t + dt) after
+    block steps (max rung 8, two steps; max rung 1, one step) against the
+    reference's output."""
+    d = load_golden("block4k.npz")
+    G, eps, th, dt, eta = (float(d[k]) for k in ("G", "eps", "theta", "dt", "eta"))
+    st0 = tuple(d[k] for k in ("x", "y", "z", "vx", "vy", "vz"))
+    for tag in ("r8", "r1"):
+        st, acc = st0, oracle.bh_accel(d["x"], d["y"], d["z"], d["m"], G, eps, th, 8)
+        for _ in range(int(d[f"{tag}_steps"])):
+            st, acc, rung, rmax = oracle.block_step(st, d["m"], G, eps, th, 8, dt, eta, int(d[f"{tag}_max_rung"]), acc)
+        np.testing.assert_array_equal(rung, d[f"{tag}_rung"])
+        assert rmax == d[f"{tag}_rung"].max() and rmax <= int(d[f"{tag}_max_rung"])
+        for k, got in zip(("x", "y", "z", "vx", "vy", "vz"), st):
+            want = d[f"{tag}_{k}"]
+            np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
+        for k, got in zip(("ax", "ay", "az"), acc):
+            want = d[f"{tag}_{k}"]
+            np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
+    assert len(np.unique(d["r8_rung"])) >= 3  # several rungs in use
