@@ -182,6 +182,12 @@ int ngrav_gpu_adaptive_dt(ngrav_gpu_ctx* ctx, double eta, double dt_max, double*
  * fresh acceleration.  rung_max: the largest rung used. */
 int ngrav_gpu_block_step(ngrav_gpu_ctx* ctx, double dt, double eta, int max_rung, int* rung_max);
 
+/* The frame fields of DeckSim::Snapshot (src/DeckSim.cpp:112-127): pos and
+ * vel as N x 3 FP32 rows in input order, each component the FP64 state value
+ * rounded once to FP32 (24 bytes per particle cross the bus instead of the 48
+ * of ngrav_gpu_get_state).  Either pointer may be NULL. */
+int ngrav_gpu_get_frame_f32(ngrav_gpu_ctx* ctx, float* pos, float* vel);
+
 /* System::Rungs (include/ngrav/System.hpp:203-205): each particle's rung
  * from the last block step, in input order (all zero before any). */
 int ngrav_gpu_get_rungs(ngrav_gpu_ctx* ctx, int* rung);
@@ -344,10 +350,13 @@ typedef struct ngrav_gpu_lmac_opts {
     int check_targets;     /* sampled targets of one check */
     double revert_rms;     /* rms relative force error that triggers the revert */
     int rounds;            /* walk rounds, 2..8: pairs for the network are decided between
-                            * rounds; the last round decides them geometrically */
+                            * rounds; the last round accepts the screened ones and decides
+                            * the rest geometrically */
     double screen;         /* accept a band pair without the network when the quadrupole
-                            * truncation bound on its error is at most screen x budget
-                            * (0: every band pair goes to the network) */
+                            * truncation bound on its error is at most screen x budget x
+                            * the group's smallest |a| (0: every band pair goes to the
+                            * network); the bound is loose by orders of magnitude, hence
+                            * the default 100 */
 } ngrav_gpu_lmac_opts;
 
 typedef struct ngrav_gpu_lmac_train_opts {

@@ -41,6 +41,7 @@ EXPORTS = (
     "ngrav_gpu_set_opts", "ngrav_gpu_set_particles", "ngrav_gpu_set_particles_f32", "ngrav_gpu_compute_accel",
     "ngrav_gpu_set_state", "ngrav_gpu_set_state_f32", "ngrav_gpu_set_softening", "ngrav_gpu_set_mac_alpha",
     "ngrav_gpu_block_step", "ngrav_gpu_get_rungs", "ngrav_gpu_adaptive_dt",
+    "ngrav_gpu_get_frame_f32",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
     "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
@@ -184,6 +185,7 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_set_mac_alpha.argtypes = [ctypes.c_void_p, ctypes.c_double]
     L.ngrav_gpu_adaptive_dt.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
                                         ctypes.POINTER(ctypes.c_double)]
+    L.ngrav_gpu_get_frame_f32.argtypes = [ctypes.c_void_p, _F, _F]
     L.ngrav_gpu_get_rungs.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.ngrav_gpu_block_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_int)]
@@ -355,6 +357,13 @@ class NBodySystem:
         d = ctypes.c_double()
         self._check(self.L.ngrav_gpu_adaptive_dt(self.h, float(eta), float(dt_max), ctypes.byref(d)), self.h)
         return d.value
+
+    def frame_f32(self):
+        """(pos, vel) as N x 3 float32 in input order: the deck writer's frame fields."""
+        pos = np.empty((self.n, 3), np.float32)
+        vel = np.empty((self.n, 3), np.float32)
+        self._check(self.L.ngrav_gpu_get_frame_f32(self.h, _p(pos, _F), _p(vel, _F)), self.h)
+        return pos, vel
 
     def rungs(self):
         """Each particle's rung from the last block step (input order)."""

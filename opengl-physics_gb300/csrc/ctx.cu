@@ -828,6 +828,20 @@ int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, dou
     return NGRAV_OK;
 }
 
+int ngrav_gpu_get_frame_f32(ngrav_gpu_ctx* ctx, float* pos, float* vel) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    const long long n = ctx->n;
+    float* st = reinterpret_cast<float*>(ctx->stage);  // 7n doubles hold the 6n floats
+    launch_frame_download(n, ctx->P.id, ctx->P.pos, split_of(ctx) ? ctx->P.plo : nullptr, ctx->P.vel,
+                          pos ? st : nullptr, vel ? st + 3 * n : nullptr, ctx->stream);
+    if (pos) NG_CUDA(cudaMemcpyAsync(pos, st, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vel) NG_CUDA(cudaMemcpyAsync(vel, st + 3 * n, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NGRAV_OK;
+}
+
 int ngrav_gpu_get_rungs(ngrav_gpu_ctx* ctx, int* rung) {
     if (!ctx || !rung) return NGRAV_ERR_INVALID_ARG;
     if (!ctx->have) return fail(ctx, NGRAV_ERR_NO_PARTICLES, "no particles set");

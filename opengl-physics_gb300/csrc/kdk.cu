@@ -115,6 +115,40 @@ void launch_download(long long n, const int* id, const float4* a, const float4* 
     download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, a, alo, ox, oy, oz);
 }
 
+// Frame fields in input order as N x 3 FP32 rows, each component the FP64
+// state value rounded once (the static_cast<float> of DeckSim::Snapshot).
+__global__ void frame_download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ pos,
+                                      const float4* __restrict__ plo, const float4* __restrict__ vel,
+                                      float* __restrict__ opos, float* __restrict__ ovel) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const long long i = 3LL * id[k];
+        if (opos) {
+            const float4 p = pos[k];
+            if (plo) {
+                const float4 l = plo[k];
+                opos[i + 0] = (float)((double)p.x + (double)l.x);
+                opos[i + 1] = (float)((double)p.y + (double)l.y);
+                opos[i + 2] = (float)((double)p.z + (double)l.z);
+            } else {
+                opos[i + 0] = p.x;
+                opos[i + 1] = p.y;
+                opos[i + 2] = p.z;
+            }
+        }
+        if (ovel) {
+            const float4 v = vel[k];
+            ovel[i + 0] = v.x;
+            ovel[i + 1] = v.y;
+            ovel[i + 2] = v.z;
+        }
+    }
+}
+
+void launch_frame_download(long long n, const int* id, const float4* pos, const float4* plo, const float4* vel,
+                           float* opos, float* ovel, cudaStream_t s) {
+    frame_download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, pos, plo, vel, opos, ovel);
+}
+
 __global__ void rung_download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ vel,
                                      int* __restrict__ out) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)

@@ -243,7 +243,6 @@ void free_rounds(LmacState& L) {
     for (int k = 0; k < 2; ++k) {
         dfree(L.R.active[k]);
         dfree(L.R.pend_node[k]);
-        dfree(L.R.pend_feat[k]);
         dfree(L.R.pend_next[k]);
         dfree(L.R.pend_owner[k]);
         dfree(L.R.pend_fill[k]);
@@ -268,22 +267,20 @@ int ensure_rounds(ngrav_gpu_ctx* ctx, long long groups, long long chunks) {
         NG_CUDA(dalloc(L.R.active[1], groups));
         L.gs_cap = groups;
     }
-    chunks = std::min<long long>(chunks, 0x7FFFFFF0LL / kListChunk);
+    chunks = std::min<long long>(chunks, 0x7FFFFFF0LL / kPendChunk);
     if (chunks > L.R.pend_chunk_cap) {
         for (int k = 0; k < 2; ++k) {
             dfree(L.R.pend_node[k]);
-            dfree(L.R.pend_feat[k]);
             dfree(L.R.pend_next[k]);
             dfree(L.R.pend_owner[k]);
             dfree(L.R.pend_fill[k]);
-            NG_CUDA(dalloc(L.R.pend_node[k], chunks * kListChunk));
-            NG_CUDA(dalloc(L.R.pend_feat[k], chunks * kListChunk));
+            NG_CUDA(dalloc(L.R.pend_node[k], chunks * kPendChunk));
             NG_CUDA(dalloc(L.R.pend_next[k], chunks));
             NG_CUDA(dalloc(L.R.pend_owner[k], chunks));
             NG_CUDA(dalloc(L.R.pend_fill[k], chunks));
         }
         dfree(L.R.dec);
-        NG_CUDA(dalloc(L.R.dec, chunks * kListChunk));
+        NG_CUDA(dalloc(L.R.dec, chunks * kPendChunk));
         L.R.pend_chunk_cap = (int)chunks;
     }
     return NGRAV_OK;
@@ -306,10 +303,10 @@ bool lmac_prepare(ngrav_gpu_ctx* ctx) {
     LmacState* L = ctx->lm;
     bool use = ctx->opts.mac == NGRAV_MAC_LEARNED && L && L->have_model && !L->reverted && ctx->acc_valid;
     if (use) {
-        // every group may park once per round; pools start at 64 deferred
+        // every group may park once per round; pools start at 32 deferred
         // pairs per particle (grown to what a round needs if that is short)
         const long long groups = std::max<long long>(ctx->cap_n, 1);
-        const long long est = ctx->n / 2 + 1024;
+        const long long est = ctx->n + 1024;
         if (ensure_rounds(ctx, groups, std::max<long long>(L->R.pend_chunk_cap, est)) != NGRAV_OK) use = false;
         L->R.rounds = std::max(2, std::min(kLmMaxRounds, L->opts.rounds));
     }
@@ -370,7 +367,7 @@ int lmac_grow_pools(ngrav_gpu_ctx* ctx) {
     NG_CUDA(cudaMemcpy(ctr, L.R.ctr, sizeof(ctr), cudaMemcpyDeviceToHost));
     long long need = 0;
     for (int r = 0; r < kLmMaxRounds; ++r) need = std::max<long long>(need, ctr[4 * r + 2]);
-    if (need >= 0x7FFFFFF0LL / kListChunk) return fail(ctx, NGRAV_ERR_CAPACITY, "deferred-pair pool exhausted");
+    if (need >= 0x7FFFFFF0LL / kPendChunk) return fail(ctx, NGRAV_ERR_CAPACITY, "deferred-pair pool exhausted");
     return ensure_rounds(ctx, L.gs_cap, std::max<long long>(need + need / 4 + 1024, 2LL * L.R.pend_chunk_cap));
 }
 
@@ -422,7 +419,7 @@ int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o) {
     o->check_targets = 4096;
     o->revert_rms = 1e-3;
     o->rounds = 3;
-    o->screen = 10.0;
+    o->screen = 100.0;
     return NGRAV_OK;
 }
 

@@ -31,14 +31,16 @@ struct LmacGroupState {
 };
 
 constexpr int kLmMaxRounds = 8;
+// Deferred pairs are kept in chunks of one warp's width: a group that parks
+// a few pairs wastes at most 31 slots of the tensor-core tiles.
+constexpr int kPendChunk = 32;
 // Per round r: ctr[4r] walk scheduler, ctr[4r+1] groups deferred, ctr[4r+2]
 // pending chunks taken, ctr[4r+3] unused.
 struct LmacRounds {
     int rounds;                        // rounds this evaluation runs (the last decides geometrically)
     LmacGroupState* gs;                // per group index
     int* active[2];                    // group indices with deferred pairs (ping-pong by round parity)
-    int* pend_node[2];                 // deferred node ids, chunks of kListChunk (ping-pong)
-    uint4* pend_feat[2];               // their standardised features, 8 x BF16 per entry
+    int* pend_node[2];                 // deferred node ids, chunks of kPendChunk (ping-pong)
     int* pend_next[2];                 // chunk links
     int* pend_owner[2];                // chunk -> group leaf
     int* pend_fill[2];                 // chunk -> entries used

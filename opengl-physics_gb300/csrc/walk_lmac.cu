@@ -6,17 +6,20 @@
 // an internal node replaced:
 //   worst <= 0 or 2h >= rho_hi * worst   -> open
 //   2h <= rho_lo * worst                 -> accept (far)
+//   quadrupole error bound within screen x budget x amin -> accept (far)
 //   otherwise                            -> the network decides
 // Round r of the walk (walk_lmac_round_kernel) resolves the group's deferred
 // pairs of round r-1 (accept -> far list, open -> children onto the stack),
 // then walks until its stack is empty, deferring every pair for the network
-// into a chunked per-group pending list.  Between rounds, lmac_infer_kernel
-// evaluates every deferred pair of the round on the tensor cores
-// (lmac_tc.cuh, 256 pairs per CTA flush) and stores the decision: accept iff
-// the logit z > gate, open iff z < -gate, the geometric test with the run's
-// theta otherwise.  The last round decides its band pairs geometrically, so
-// every group's lists are complete after it.  Traversal warps never wait for
-// the tensor cores, and the tensor-core kernel runs as a streaming batch.
+// (its node id, with the geometric decision in the top bit) into a chunked
+// per-group pending list.  Between rounds, lmac_infer_kernel gathers the
+// deferred pairs' records, computes their features and evaluates the network
+// on the tensor cores (lmac_tc.cuh, 256 pairs per CTA flush), and stores the
+// decision: accept iff the logit z > gate, open iff z < -gate, the geometric
+// test with the run's theta otherwise.  The last round decides its band pairs
+// by the bound and the geometric test, so every group's lists are complete
+// after it.  Traversal warps never wait for the tensor cores, and the
+// tensor-core kernel runs as a streaming batch.
 //
 // lmac_tc_forward_kernel evaluates the same network routine on given features
 // (the unit test of the tensor-core path against the oracle).
@@ -35,7 +38,7 @@ constexpr int kLwStack = 2048;  // per-warp shared-memory traversal stack
 // Append to a group's deferred-pair list: chunks taken one at a time (so
 // every chunk counted is owned and filled), owner and fill recorded for the
 // tensor-core kernel.
-__device__ __forceinline__ void pend_append(ChunkList& L, bool has, int val, uint4 feat, const LmacRounds& R, int out,
+__device__ __forceinline__ void pend_append(ChunkList& L, bool has, int val, const LmacRounds& R, int out,
                                             int* counter, int leaf, int lane, unsigned lt_mask, unsigned& bad) {
     const unsigned m = __ballot_sync(0xffffffffu, has);
     const int k = __popc(m);
@@ -51,12 +54,12 @@ __device__ __forceinline__ void pend_append(ChunkList& L, bool has, int val, uin
         L.pos = 0;
     }
     int newc = -1;
-    if (L.pos + k > kListChunk) {
+    if (L.pos + k > kPendChunk) {
         if (lane == 0) {
             newc = atomicAdd(counter, 1);
             if (L.cur < cap) {
                 R.pend_next[out][L.cur] = newc;
-                R.pend_fill[out][L.cur] = kListChunk;
+                R.pend_fill[out][L.cur] = kPendChunk;
             }
             if (newc < cap) R.pend_owner[out][newc] = leaf;
         }
@@ -64,18 +67,17 @@ __device__ __forceinline__ void pend_append(ChunkList& L, bool has, int val, uin
     }
     if (has) {
         const int i = L.pos + __popc(m & lt_mask);
-        const int c = i < kListChunk ? L.cur : newc;
-        const int p = i < kListChunk ? i : i - kListChunk;
+        const int c = i < kPendChunk ? L.cur : newc;
+        const int p = i < kPendChunk ? i : i - kPendChunk;
         if (c < cap) {
-            R.pend_node[out][(long long)c * kListChunk + p] = val;
-            R.pend_feat[out][(long long)c * kListChunk + p] = feat;
+            R.pend_node[out][(long long)c * kPendChunk + p] = val;
         } else {
             bad |= kStPendOverflow;
         }
     }
     if (newc >= 0) {
         L.cur = newc;
-        L.pos = L.pos + k - kListChunk;
+        L.pos = L.pos + k - kPendChunk;
     } else {
         L.pos += k;
     }
@@ -119,7 +121,6 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
     int* active_out = R.active[out];
     int* pend_ctr = R.ctr + 4 * round + 2;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const float eps = sqrtf(wp.eps2);
     unsigned long long tests = 0, groups = 0, resolved = 0, screened = 0;
     int stack_max = 0, list_max = 0;
     unsigned bad = 0;
@@ -156,13 +157,13 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
             // resolve the deferred pairs of the previous round, 32 at a time
             int chunk = g.pend_first;
             for (int i0 = 0; i0 < g.pend_count; i0 += 32) {
-                const int e = (i0 & (kListChunk - 1)) + lane;
+                const int e = (i0 & (kPendChunk - 1)) + lane;
                 const bool has = i0 + lane < g.pend_count;
                 int node = -1, nch = 0, link = 0;
                 bool acc = false;
                 if (has) {
-                    const long long slot = (long long)chunk * kListChunk + e;
-                    node = R.pend_node[in][slot];
+                    const long long slot = (long long)chunk * kPendChunk + e;
+                    node = R.pend_node[in][slot] & 0x7FFFFFFF;
                     acc = R.dec[slot] != 0;
                     if (!acc) {
                         const float4 Cw = T.wC[node];
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                 }
                 for (int q = 0; q < nch; ++q) stack[size + off + q] = link + q;
                 size += tot;
-                if (((i0 + 32) & (kListChunk - 1)) == 0 && i0 + 32 < g.pend_count) chunk = R.pend_next[in][chunk];
+                if (((i0 + 32) & (kPendChunk - 1)) == 0 && i0 + 32 < g.pend_count) chunk = R.pend_next[in][chunk];
             }
             __syncwarp();
         }
@@ -200,32 +201,25 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                 const int idx = lane + 32 * q;
                 node[q] = idx < take ? stack[size + idx] : -1;
             }
-            float4 A[2], Cw[2], D[2], B[2];
-            int cnt[2];
+            float4 A[2], Cw[2], D[2];
 #pragma unroll
             for (int q = 0; q < 2; ++q) {  // every record in flight at once
                 if (node[q] >= 0) {
                     A[q] = T.wA[node[q]];
                     Cw[q] = T.wC[node[q]];
                     D[q] = T.wD[node[q]];
-                    B[q] = T.wB[node[q]];
-                    cnt[q] = T.count[node[q]];
                 } else {
                     A[q] = make_float4(0.f, 0.f, 0.f, 0.f);
                     Cw[q] = A[q];
                     D[q] = A[q];
-                    B[q] = A[q];
-                    cnt[q] = 0;
                 }
             }
             __syncwarp();
             int kind[2], nch[2], link[2];
-            uint4 row[2];
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 kind[q] = 0;  // 0 none, 1 near, 2 far, 3 open, 4 deferred
                 nch[q] = 0;
-                row[q] = make_uint4(0u, 0u, 0u, 0u);
                 link[q] = __float_as_int(Cw[q].z);
                 const int meta = __float_as_int(Cw[q].w);
                 if (node[q] >= 0 && node[q] != leaf && A[q].w > 0.f) {
@@ -241,12 +235,13 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                             kind[q] = 3;
                         } else if (sz <= wp.lm_rho_lo * worst) {
                             kind[q] = 2;
-                        } else if (!last) {
-                            kind[q] = 4;
+                        } else {
+                            // the network (rounds before the last) or the geometric test
+                            kind[q] = !last ? 4 : (sz * sz < wp.theta2 * worst * worst ? 2 : 3);
                             // Quadrupole truncation bound on every member (Salmon & Warren
                             // 1994, p = 2): |da| <= G M / w^2 * 4 x^3 / (1 - x)^2, x = maxR / w.
                             const float x = Cw[q].x / worst;
-                            if (wp.lm_screen > 0.f && x < 1.f) {
+                            if (kind[q] != 2 && wp.lm_screen > 0.f && x < 1.f) {
                                 const float om = 1.f - x;
                                 const float bound = wp.G * A[q].w / (worst * worst) * 4.f * x * x * x / (om * om);
                                 if (bound <= wp.lm_screen * wp.lm_budget * amin) {
@@ -254,16 +249,11 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                                     ++screened;
                                 }
                             }
-                        } else {
-                            kind[q] = sz * sz < wp.theta2 * worst * worst ? 2 : 3;
                         }
                         if (kind[q] == 3) nch[q] = meta & 0xFFFFFF;
-                        if (kind[q] == 4) {
-                            float f[kLmacIn];
-                            lmac_features(gA, gD, gR, amin, A[q], B[q], Cw[q], D[q], cnt[q], wp.G, eps, wp.lm_log2b,
-                                          f);
-                            row[q] = lmac_row(f, wp);
-                        }
+                        // the geometric decision rides in the deferred node id's top
+                        // bit for the low-confidence fallback
+                        if (kind[q] == 4 && sz * sz < wp.theta2 * worst * worst) node[q] |= (int)0x80000000u;
                     }
                 }
             }
@@ -274,7 +264,7 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                             LB.near_chunk_cap, lane, lt_mask, bad);
                 list_append(far, kind[q] == 2, node[q], LB.far, LB.far_next, &C->far_chunks, LB.far_chunk_cap,
                             lane, lt_mask, bad);
-                pend_append(pend, kind[q] == 4, node[q], row[q], R, out, pend_ctr, leaf, lane, lt_mask, bad);
+                pend_append(pend, kind[q] == 4, node[q], R, out, pend_ctr, leaf, lane, lt_mask, bad);
             }
             bool ovf = false;
 #pragma unroll
@@ -336,10 +326,12 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
     (void)resolved;
 }
 
-// Decide every deferred pair of `round`: pairs of chunks 2t and 2t+1 form
-// tile t (entry e of chunk 2t+h is pair slot 32h + (e % 32) of warp e / 32).
-// The walk stored each pair's operand row; a CTA streams its tiles, loading
-// the next tile's rows while the current one is on the tensor cores.
+// Decide every deferred pair of `round`: chunks 8t .. 8t+7 form tile t
+// (entry l of chunk 8t + 2w + h is pair slot 32h + l of warp w).  Each
+// thread gathers its two pairs' records (the node's, and its chunk's group
+// leaf's), computes the features and writes the operand rows; the ids of the
+// CTA's next tile are in flight meanwhile, and the CTAs sharing an SM overlap
+// one another's gathers with their tensor-core work.
 __global__ void __launch_bounds__(kLwThreads) lmac_infer_kernel(NodeArrays T, Counters* C, WalkParams wp,
                                                                 LmacRounds R, int round,
                                                                 const LmacDev* __restrict__ model) {
@@ -347,7 +339,6 @@ __global__ void __launch_bounds__(kLwThreads) lmac_infer_kernel(NodeArrays T, Co
     LmacTiles& S = *lmac_tiles_at(lm_dyn);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int e = threadIdx.x;  // entry within a chunk
     __shared__ unsigned s_status;
     if (threadIdx.x == 0) s_status = C->status;
     __syncthreads();
@@ -355,50 +346,58 @@ __global__ void __launch_bounds__(kLwThreads) lmac_infer_kernel(NodeArrays T, Co
     const int pool = round & 1;
     int nchunks = R.ctr[4 * round + 2];
     nchunks = nchunks < R.pend_chunk_cap ? nchunks : R.pend_chunk_cap;
-    const int ntiles = (nchunks + 1) / 2;
+    const int ntiles = (nchunks + 7) / 8;  // a tile: 8 chunks, two per warp
     if ((int)blockIdx.x >= ntiles) return;
     lmac_tc_init(S, model);
-    const uint4* feat = R.pend_feat[pool];
+    const int* pnode = R.pend_node[pool];
     const int* fill = R.pend_fill[pool];
+    const int* owner = R.pend_owner[pool];
+    const float eps = sqrtf(wp.eps2);
     unsigned char* a1 = reinterpret_cast<unsigned char*>(S.a2);
     uint32_t phase = 0;
     bool ok_all = true;
     unsigned long long queries = 0, accepts = 0, fallbacks = 0, flushes = 0;
-    // Rows are loaded without waiting for the fill counts (slots past a
-    // chunk's fill hold stale rows whose logits are never used).
-    auto load_tile = [&](int t, uint4 rows[2], int fills[2]) {
+    // ids of a tile: node (top bit: the geometric decision), owner leaf, or
+    // -1 past a chunk's fill
+    auto load_ids = [&](int t, int nd[2], int lf[2]) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int c = 2 * t + h;
-            const bool in = c < nchunks;
-            fills[h] = in ? fill[c] : 0;
-            rows[h] = in ? feat[(long long)c * kListChunk + e] : make_uint4(0u, 0u, 0u, 0u);
+            const int c = 8 * t + 2 * warp + h;
+            const bool in = c < nchunks && lane < fill[c];
+            nd[h] = in ? pnode[(long long)c * kPendChunk + lane] : 0;
+            lf[h] = in ? owner[c] : -1;
         }
     };
-    uint4 rows[2];
-    int fills[2];
+    int nd[2], lf[2];
     int t = blockIdx.x;
-    load_tile(t, rows, fills);
+    load_ids(t, nd, lf);
     for (; t < ntiles; t += gridDim.x) {
+        const int cnd[2] = {nd[0], nd[1]}, clf[2] = {lf[0], lf[1]};
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
-            *reinterpret_cast<uint4*>(a1 + tc::kmajor_offset(32 * warp + lane, 8 * h, kA1Lbo, kA1Sbo)) = rows[h];
-        const bool cur_valid[2] = {e < fills[0], e < fills[1]};
-        if (t + (int)gridDim.x < ntiles) load_tile(t + gridDim.x, rows, fills);  // in flight during the MMAs
+        for (int h = 0; h < 2; ++h) {
+            uint4 row = make_uint4(0u, 0u, 0u, 0u);
+            if (clf[h] >= 0) {
+                const int node = cnd[h] & 0x7FFFFFFF, leaf = clf[h];
+                float f[kLmacIn];
+                lmac_features(T.wA[leaf], T.wD[leaf], T.wC[leaf].x, T.amin[leaf], T.wA[node], T.wB[node],
+                              T.wC[node], T.wD[node], T.count[node], wp.G, eps, wp.lm_log2b, f);
+                row = lmac_row(f, wp);
+            }
+            *reinterpret_cast<uint4*>(a1 + tc::kmajor_offset(32 * warp + lane, 8 * h, kA1Lbo, kA1Sbo)) = row;
+        }
+        if (t + (int)gridDim.x < ntiles) load_ids(t + gridDim.x, nd, lf);  // in flight during the MMAs
         float z[2];
         ok_all = lmac_tc_flush(S, warp, lane, phase, z[0], z[1]) && ok_all;
         ++flushes;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            if (!cur_valid[h]) continue;
-            const long long slot = (long long)(2 * t + h) * kListChunk + e;
+            if (clf[h] < 0) continue;
+            const long long slot = (long long)(8 * t + 2 * warp + h) * kPendChunk + lane;
             bool acc;
             if (fabsf(z[h]) >= wp.lm_gate) {
                 acc = z[h] > 0.f;
-            } else {  // low confidence: the geometric test decides
-                const int nd = R.pend_node[pool][slot];
-                const int leaf = R.pend_owner[pool][2 * t + h];
-                acc = geometric_accept(T.wA[nd], T.wC[nd], T.wD[nd], T.wA[leaf], T.wD[leaf], T.wC[leaf].x, wp.theta2);
+            } else {  // low confidence: the geometric test decides (recorded by the walk)
+                acc = cnd[h] < 0;
                 ++fallbacks;
             }
             ++queries;

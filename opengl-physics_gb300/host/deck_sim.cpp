@@ -140,18 +140,11 @@ void DeckSim::Step(int substeps) {
 
 void DeckSim::Snapshot(fw::OutputWriter& writer) {
     const size_t n = (size_t)m_n;
-    std::vector<double> x(n), y(n), z(n), vx(n), vy(n), vz(n);
-    Check(ngrav_gpu_get_state(m_ctx, x.data(), y.data(), z.data(), vx.data(), vy.data(), vz.data()),
-          "ngrav_gpu_get_state");
-    std::vector<float> pos(n * 3), vel(n * 3);
-    for (size_t i = 0; i < n; ++i) {
-        pos[i * 3 + 0] = (float)x[i];
-        pos[i * 3 + 1] = (float)y[i];
-        pos[i * 3 + 2] = (float)z[i];
-        vel[i * 3 + 0] = (float)vx[i];
-        vel[i * 3 + 1] = (float)vy[i];
-        vel[i * 3 + 2] = (float)vz[i];
-    }
+    m_pos.resize(n * 3);
+    m_vel.resize(n * 3);
+    std::vector<float>& pos = m_pos;
+    std::vector<float>& vel = m_vel;
+    Check(ngrav_gpu_get_frame_f32(m_ctx, pos.data(), vel.data()), "ngrav_gpu_get_frame_f32");
     writer.WriteField("pos", pos.data(), fw::NpyDtype::F4, (int)n, 3);
     writer.WriteField("vel", vel.data(), fw::NpyDtype::F4, (int)n, 3);
 

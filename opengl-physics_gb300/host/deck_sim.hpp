@@ -57,6 +57,7 @@ private:
     int m_blockMaxRung = 8;
     int m_rungMax = 0;
     std::vector<std::string> m_warnings;
+    std::vector<float> m_pos, m_vel;  // frame buffers, reused across snapshots
 };
 
 }  // namespace ngrav_host

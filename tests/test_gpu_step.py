@@ -119,3 +119,17 @@ def test_set_state_replaces_positions_and_keeps_accelerations(pkg):
         b.step(2, dt)
         for u, v in zip(a.state(), b.state()):
             np.testing.assert_allclose(u, v, rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("precision", ["split", "plain"])
+def test_frame_f32_is_the_rounded_state(pkg, precision):
+    """The deck writer's frame readback equals the FP64 state rounded once to
+    FP32 (DeckSim::Snapshot's static_cast<float>), in input order."""
+    d = load_golden("plummer16k.npz")
+    with sim_for(pkg, d, precision) as sim:
+        sim.prime()
+        sim.step(3, float(d["dt"]))
+        st = sim.state()
+        pos, vel = sim.frame_f32()
+    np.testing.assert_array_equal(pos, np.stack(st[0:3], 1).astype(np.float32))
+    np.testing.assert_array_equal(vel, np.stack(st[3:6], 1).astype(np.float32))
