@@ -11,10 +11,12 @@ walk with P2P/P2C, closing kick) over the whole system.
 
 Headline: the learned opening test against the plain theta test at equal
 rms relative force error (1e-3, FP64-summed direct sum on 4,096 targets).
-Setup, untimed: the network is trained on the run itself (16 snapshots,
-2^22 labelled pairs), theta and the learned budget are each set to the
-largest grid value whose error stays within the target.  Then both arms
-step the same system K times.
+Setup, untimed: for each leaf capacity of --leaf-grid (the target-group
+size), the network is trained on the run itself (16 snapshots, 2^22
+labelled pairs), and theta and the learned budget are each set to the
+largest grid value whose error stays within the target; each arm then runs
+at the leaf capacity whose calibrated evaluation is fastest.  Both arms
+step the same input state K times.
 
 value   = N * K / (device time of the learned arm's K timed steps, CUDA
           events on the engine's stream), inputs resident in HBM; the theta
@@ -274,6 +276,8 @@ def main():
     ap.add_argument("--lmac-pairs", type=int, default=1 << 22)
     ap.add_argument("--lmac-snapshots", type=int, default=16)
     ap.add_argument("--precision", default="split", choices=["split", "plain"])
+    ap.add_argument("--leaf-grid", default="16,24,32,48",
+                    help="leaf capacities tried per arm (comma list; one value fixes it)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -295,27 +299,62 @@ def main():
     sim.prime()
     learned = args.mac == "learned"
 
-    # ---- setup (untimed): train on the run itself, calibrate both tests ----
-    train, cal_theta, cal_budget = None, None, None
-    if learned:
-        t0 = time.perf_counter()
-        train = sim.lmac_train(snapshots=args.lmac_snapshots, steps_between=1, dt=dt, pairs=args.lmac_pairs,
-                               epochs=4, batch=8192, seed=1)
-        train["wall_s"] = time.perf_counter() - t0
-    if args.theta is None:
-        theta, cal_theta = calibrate(sim, THETA_GRID, lambda v: sim.set_opts(theta=v, mac=pkg.MAC_GEOMETRIC))
-    else:
-        theta = args.theta
-    sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
-    budget = None
-    if learned:
-        def set_budget(v):
-            sim.set_opts(mac=pkg.MAC_LEARNED)
-            sim.lmac_set_opts(budget=v, check_every=0)
-        if args.budget is None:
-            budget, cal_budget = calibrate(sim, BUDGET_GRID, set_budget)
+    # ---- setup (untimed): per leaf capacity (the target-group size), train
+    # on the run itself and calibrate both tests to the error target; each arm
+    # then runs at its own fastest leaf capacity ----
+    leaf_grid = [int(v) for v in args.leaf_grid.split(",")] if args.leaf_grid else [ncrit]
+
+    def restart(L):
+        sim.set_opts(leaf_capacity=L, mac=pkg.MAC_GEOMETRIC)
+        sim.set_particles_f32(*arrs)
+        sim.prime()
+
+    def eval_ms(reps=3):
+        ms = 0.0
+        for _ in range(reps):
+            sim.compute_accel()
+            ms += sum(phases(sim.stats()).values())
+        return ms / reps
+
+    def set_budget(v):
+        sim.set_opts(mac=pkg.MAC_LEARNED)
+        sim.lmac_set_opts(budget=v, check_every=0)
+
+    tuning = []
+    for L in leaf_grid:
+        row = {"leaf_capacity": L}
+        restart(L)
+        if args.theta is None:
+            row["theta"], row["cal_theta"] = calibrate(sim, THETA_GRID,
+                                                       lambda v: sim.set_opts(theta=v, mac=pkg.MAC_GEOMETRIC))
         else:
-            budget = args.budget
+            row["theta"] = args.theta
+        sim.set_opts(theta=row["theta"], mac=pkg.MAC_GEOMETRIC)
+        row["ms_eval_theta"] = eval_ms()
+        if learned:
+            t0 = time.perf_counter()
+            row["train"] = sim.lmac_train(snapshots=args.lmac_snapshots, steps_between=1, dt=dt,
+                                          pairs=args.lmac_pairs, epochs=4, batch=8192, seed=1)
+            row["train"]["wall_s"] = time.perf_counter() - t0
+            row["model"] = sim.lmac_get_model()
+            restart(L)  # training stepped the system: start again from the inputs
+            sim.set_opts(theta=row["theta"])
+            if args.budget is None:
+                row["budget"], row["cal_budget"] = calibrate(sim, BUDGET_GRID, set_budget)
+            else:
+                row["budget"] = args.budget
+            set_budget(row["budget"])
+            row["ms_eval_learned"] = eval_ms()
+        tuning.append(row)
+    best_t = min(tuning, key=lambda r: r["ms_eval_theta"])
+    theta, cal_theta, ncrit_t = best_t["theta"], best_t.get("cal_theta"), best_t["leaf_capacity"]
+    budget, cal_budget, train, ncrit_l = None, None, None, ncrit_t
+    if learned:
+        best_l = min(tuning, key=lambda r: r["ms_eval_learned"])
+        budget, cal_budget, train = best_l["budget"], best_l.get("cal_budget"), best_l["train"]
+        ncrit_l = best_l["leaf_capacity"]
+    tuning_table = [{k: v for k, v in r.items() if k in ("leaf_capacity", "theta", "budget", "ms_eval_theta",
+                                                         "ms_eval_learned")} for r in tuning]
 
     dist = None
     if world > 1:
@@ -328,10 +367,11 @@ def main():
     clocks = ClockSampler(dev)
 
     # ---- geometric (plain theta) arm ----
+    restart(ncrit_t)
     sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
     st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks)
     fe_g = error_at(sim)
-    arm_theta = {"theta": theta, "value": world * n / (ms_g * 1e-3), "ms_per_step": ms_g,
+    arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "value": world * n / (ms_g * 1e-3), "ms_per_step": ms_g,
                  "force_err_rms": fe_g["rms"], "force_err_max": fe_g["max"],
                  "p2p_pairs_per_step": st_g["cum_p2p_pairs"] / max(1, st_g["cum_evals"]),
                  "p2c_terms_per_step": st_g["cum_p2c_terms"] / max(1, st_g["cum_evals"]),
@@ -341,7 +381,9 @@ def main():
 
     # ---- learned arm (the method) ----
     if learned:
-        sim.set_opts(mac=pkg.MAC_LEARNED)
+        restart(ncrit_l)
+        sim.lmac_set_model(*best_l["model"])
+        sim.set_opts(theta=best_l["theta"], mac=pkg.MAC_LEARNED)
         sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=TARGET_RMS * 1.5)
         sim.lmac_reset()
         st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks)
@@ -398,12 +440,13 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(ge.load_oracle(), arrs, eps, theta, ncrit)
+            cpu = cpu_baseline(ge.load_oracle(), arrs, eps, theta, ncrit_t)
         except Exception as exc:  # the baseline must not sink the GPU line
             cpu = {"error": str(exc)}
 
     if rank == 0:
-        cfg = {"workload": args.workload, "n": n, "mac": args.mac, "eps": eps, "dt": dt, "leaf_capacity": ncrit,
+        cfg = {"workload": args.workload, "n": n, "mac": args.mac, "eps": eps, "dt": dt,
+               "leaf_capacity": ncrit_l if learned else ncrit_t, "leaf_capacity_tuning": tuning_table,
                "precision": args.precision, "quadrupole": True, "target_rms": TARGET_RMS,
                "parallelism": "replicas" if world > 1 else "single-gpu",
                "l2": "per-step working set > 0.5 GB, larger than the 129 MB L2",

@@ -354,7 +354,7 @@ void lmac_launch_walk(ngrav_gpu_ctx* ctx, const WalkParams& wp, const void* mode
     cudaStream_t s = ctx->stream;
     cudaMemsetAsync(L.R.ctr, 0, sizeof(int) * 4 * kLmMaxRounds, s);
     for (int r = 0; r < L.R.rounds; ++r) {
-        launch_walk_lmac_round(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, L.R, r, s);
+        launch_walk_lmac_round(ctx->T, ctx->C, ctx->leaf_list, wp, ctx->LB, L.R, r, ctx->sm_count, s);
         if (r + 1 < L.R.rounds)
             launch_lmac_infer(ctx->T, ctx->C, wp, L.R, r, static_cast<const LmacDev*>(model), ctx->sm_count, s);
     }

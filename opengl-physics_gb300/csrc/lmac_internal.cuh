@@ -50,7 +50,7 @@ struct LmacRounds {
 };
 
 void launch_walk_lmac_round(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
-                            const ListBuffers& LB, const LmacRounds& R, int round, cudaStream_t s);
+                            const ListBuffers& LB, const LmacRounds& R, int round, int sm_count, cudaStream_t s);
 void launch_lmac_infer(const NodeArrays& T, Counters* C, const WalkParams& wp, const LmacRounds& R, int round,
                        const LmacDev* model, int sm_count, cudaStream_t s);
 void launch_lmac_tc_forward(const LmacDev* model, const float* X, int n, float* z, unsigned* status, int sm_count,

@@ -33,7 +33,9 @@ namespace ngrav {
 
 constexpr int kLwWarps = 4;
 constexpr int kLwThreads = kLwWarps * 32;
-constexpr int kLwStack = 2048;  // per-warp shared-memory traversal stack
+// Per-warp shared-memory traversal stack: 2048 entries at 6 CTAs per SM, or
+// 1024 at 8 (the walk_stack tuning knob picks; an overflow moves the run to
+// the global-memory stack).
 
 // Append to a group's deferred-pair list: chunks taken one at a time (so
 // every chunk counted is owned and filled), owner and fill recorded for the
@@ -103,17 +105,18 @@ __device__ __forceinline__ bool geometric_accept(const float4 A, const float4 Cw
     return worst > 0.f && Cw.y * Cw.y < theta2 * worst * worst;
 }
 
-template <bool SMEM_STACK>
-__global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArrays T, Counters* C,
-                                                                     const int* __restrict__ leaf_list,
-                                                                     WalkParams wp, ListBuffers LB, LmacRounds R,
-                                                                     int round) {
-    __shared__ int s_stack[SMEM_STACK ? kLwWarps * kLwStack : 1];
+template <int STACK, int MINB>
+__global__ void __launch_bounds__(kLwThreads, MINB) walk_lmac_round_kernel(NodeArrays T, Counters* C,
+                                                                        const int* __restrict__ leaf_list,
+                                                                        WalkParams wp, ListBuffers LB, LmacRounds R,
+                                                                        int round) {
+    // STACK = 0: the global-memory stack of LB
+    __shared__ int s_stack[STACK > 0 ? kLwWarps * STACK : 1];
     const int lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * kLwWarps + (threadIdx.x >> 5);
     if (C->status & kStFatal) return;
-    int* stack = SMEM_STACK ? s_stack + (threadIdx.x >> 5) * kLwStack : LB.stack + (long long)gwarp * LB.stack_cap;
-    const int stack_cap = SMEM_STACK ? kLwStack : LB.stack_cap;
+    int* stack = STACK > 0 ? s_stack + (threadIdx.x >> 5) * STACK : LB.stack + (long long)gwarp * LB.stack_cap;
+    const int stack_cap = STACK > 0 ? STACK : LB.stack_cap;
     const bool last = round == R.rounds - 1;
     const int in = (round + 1) & 1, out = round & 1;
     const int ngroups = round == 0 ? C->nleaves : R.ctr[4 * (round - 1) + 1];
@@ -121,6 +124,7 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
     int* active_out = R.active[out];
     int* pend_ctr = R.ctr + 4 * round + 2;
     const unsigned lt_mask = (1u << lane) - 1u;
+    const float four_g = 4.f * wp.G;
     unsigned long long tests = 0, groups = 0, resolved = 0, screened = 0;
     int stack_max = 0, list_max = 0;
     unsigned bad = 0;
@@ -137,6 +141,7 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
         const float4 gD = T.wD[leaf];
         const float gR = T.wC[leaf].x;
         const float amin = T.amin[leaf];
+        const float screen_b = wp.lm_screen * wp.lm_budget * amin;  // 0: no screen
         ChunkList far, near, pend = {-1, -1, 0, 0, 0, 0};
         int size = 0;
         if (round == 0) {
@@ -239,15 +244,13 @@ __global__ void __launch_bounds__(kLwThreads, 6) walk_lmac_round_kernel(NodeArra
                             // the network (rounds before the last) or the geometric test
                             kind[q] = !last ? 4 : (sz * sz < wp.theta2 * worst * worst ? 2 : 3);
                             // Quadrupole truncation bound on every member (Salmon & Warren
-                            // 1994, p = 2): |da| <= G M / w^2 * 4 x^3 / (1 - x)^2, x = maxR / w.
-                            const float x = Cw[q].x / worst;
-                            if (kind[q] != 2 && wp.lm_screen > 0.f && x < 1.f) {
-                                const float om = 1.f - x;
-                                const float bound = wp.G * A[q].w / (worst * worst) * 4.f * x * x * x / (om * om);
-                                if (bound <= wp.lm_screen * wp.lm_budget * amin) {
-                                    kind[q] = 2;
-                                    ++screened;
-                                }
+                            // 1994, p = 2): |da| <= G M / w^2 * 4 x^3 / (1 - x)^2, x = r / w,
+                            // r = maxR; tested as 4 G M r^3 <= screen b amin w^3 (w - r)^2.
+                            const float r = Cw[q].x, wr = worst - r;
+                            if (kind[q] != 2 && screen_b > 0.f && wr > 0.f &&
+                                four_g * A[q].w * (r * r * r) <= screen_b * (worst * worst * worst) * (wr * wr)) {
+                                kind[q] = 2;
+                                ++screened;
                             }
                         }
                         if (kind[q] == 3) nch[q] = meta & 0xFFFFFF;
@@ -466,12 +469,17 @@ void lmac_set_attributes() {
 }
 
 void launch_walk_lmac_round(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
-                            const ListBuffers& LB, const LmacRounds& R, int round, cudaStream_t s) {
-    const int blocks = (LB.nwarps + kLwWarps - 1) / kLwWarps;
-    if (wp.global_stack)
-        walk_lmac_round_kernel<false><<<blocks, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
-    else
-        walk_lmac_round_kernel<true><<<blocks, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+                            const ListBuffers& LB, const LmacRounds& R, int round, int sm_count, cudaStream_t s) {
+    // persistent warps: one wave of resident CTAs (the global-stack variant
+    // has one stack per warp of LB)
+    if (wp.global_stack) {
+        const int blocks = (LB.nwarps + kLwWarps - 1) / kLwWarps;
+        walk_lmac_round_kernel<0, 6><<<blocks, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+    } else if (wp.smem_stack == 1024) {
+        walk_lmac_round_kernel<1024, 8><<<sm_count * 8, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+    } else {
+        walk_lmac_round_kernel<2048, 6><<<sm_count * 6, kLwThreads, 0, s>>>(T, C, leaf_list, wp, LB, R, round);
+    }
 }
 
 void launch_lmac_infer(const NodeArrays& T, Counters* C, const WalkParams& wp, const LmacRounds& R, int round,
