@@ -15,8 +15,9 @@
 // the group's frame, the next batch loading into registers while this one is
 // evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
 // per leaf, completing on an mbarrier with a bounded wait) into a 4 KiB
-// shared-memory buffer, batches of leaves sized by the leaf capacity; the
-// next batch's leaf records load while a batch is in flight.  (A second
+// shared-memory buffer, each batch as many leaves (up to 32) as fit by
+// their actual counts; the next batch's leaf records load while a batch is
+// in flight.  (A second
 // buffer would overlap copy and compute within the warp, but halves the
 // resident warps; measured slower.)  In SPLIT precision each lane's partial
 // sums are Kahan compensated once per staged chunk.
@@ -214,7 +215,7 @@ __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA
     accumulate<SPLIT>(g, px, py, pz);
 }
 
-// One near batch's info, loaded into registers by lanes e < be.
+// One near leaf's info (lane = list entry), loaded into registers.
 struct NearInfo {
     int start, cnt;
     float4 shift;
@@ -264,6 +265,33 @@ __device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& 
     return tot;
 }
 
+// Info of near-list entries pos .. pos+31 (lane = entry), which may run
+// into the next 128-entry chunk; lanes past the list get count 0.
+template <bool SPLIT>
+__device__ __forceinline__ NearInfo load_near_batch(const NodeArrays& T, const ListBuffers& LB, int chunk, int pos,
+                                                    int lane, int nnear, const float4& gchi, const float4& gclo) {
+    const int e = pos + lane;
+    const bool valid = e < nnear;
+    const bool next = (pos & (kListChunk - 1)) + lane >= kListChunk;
+    int c = chunk;
+    if (valid && next) c = LB.near_next[chunk];
+    return load_near_info<SPLIT>(T, LB, c, e, valid, gchi, gclo);
+}
+
+// Stage the longest prefix of the 32 leaves in `in` whose sources fit `cap`
+// (at least one: every leaf fits the buffer outside the big-leaf path).
+// Returns the staged source count; nb = leaves staged.
+__device__ __forceinline__ int stage_fitting(EvalSmem& sm, const NearInfo& in, int lane,
+                                             const float4* __restrict__ src, int cap, int& nb) {
+    int tot;
+    const int ex = excl_scan(in.cnt, lane, tot);
+    const bool fits = ex + in.cnt <= cap || lane == 0;
+    nb = __popc(__ballot_sync(0xffffffffu, fits));  // counts are >= 0: a prefix of lanes
+    NearInfo mine = in;
+    if (lane >= nb) mine.cnt = 0;
+    return stage_batch(sm, 0, mine, lane, src);
+}
+
 template <bool SPLIT, bool QUAD, int SOFT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
@@ -281,13 +309,9 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
     __syncwarp();
     unsigned phase[2] = {0u, 0u};
     const int nleaves = C->nleaves;
-    // Leaves per near batch: the largest power of two whose worst-case
-    // source count fits one staging buffer (so a batch never straddles a
-    // 128-entry list chunk).
+    // Sources per near batch: the tuned cap (at most one staging buffer).
     const int maxleaf = max(1, C->max_leaf_count);
-    const int tile = wp.p2p_tile > 0 && wp.p2p_tile < kSrcCap ? wp.p2p_tile : kSrcCap;  // tuned batch cap
-    int be = 1;
-    while (be < 32 && (be * 2) * maxleaf <= tile) be *= 2;
+    const int tile = wp.p2p_tile > 0 && wp.p2p_tile < kSrcCap ? wp.p2p_tile : kSrcCap;
     const bool big_leaves = maxleaf > kSrcCap;
     unsigned long long pairs = 0, p2c = 0;
     bool timeout = false;
@@ -361,62 +385,52 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
             }
             p2c += (unsigned long long)g.nt * (unsigned long long)nfar;
 
-            // ---- near field: batches of `be` leaves staged by TMA, double-buffered ----
+            // ---- near field: batches of up to 32 leaves (as many as fit the
+            // staging buffer, by their actual counts) staged by TMA ----
             int total = 0;
             if (!big_leaves) {
-                const int nbatch = (nnear + be - 1) / be;
-                int chunk_pf = near_first;  // list chunk of the batch being prefetched
-                NearInfo info = load_near_info<SPLIT>(T, LB, chunk_pf, lane, lane < be && lane < nnear, gchi, gclo);
-                int ns_cur = stage_batch(sm, 0, info, lane, src);
-                if (nbatch > 1) {
-                    const int i1 = be;
-                    if ((i1 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
-                    info = load_near_info<SPLIT>(T, LB, chunk_pf, i1 + lane, lane < be && i1 + lane < nnear, gchi,
-                                                 gclo);
+                int pos = 0;               // list index of the batch's first leaf
+                int chunk = near_first;    // list chunk holding entry `pos`
+                NearInfo info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
+                int nb = 0;
+                int ns_cur = stage_fitting(sm, info, lane, src, tile, nb);
+                pos += nb;
+                if (pos < nnear) {
+                    if ((pos & (kListChunk - 1)) < nb) chunk = LB.near_next[chunk];  // crossed a chunk boundary
+                    info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
                 }
-                for (int k = 0; k < nbatch; ++k) {
-                    const int bcur = kBuffers == 2 ? (k & 1) : 0;
-                    int ns_next = 0;
-                    if (kBuffers == 2 && k + 1 < nbatch) {
-                        ns_next = stage_batch(sm, bcur ^ 1, info, lane, src);
-                        const int i2 = (k + 2) * be;
-                        if (k + 2 < nbatch) {
-                            if ((i2 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
-                            info = load_near_info<SPLIT>(T, LB, chunk_pf, i2 + lane, lane < be && i2 + lane < nnear,
-                                                         gchi, gclo);
+                int nb_cur = nb;
+                while (ns_cur > 0) {
+                    if (!mbar_wait(&sm.bar[0], phase[0])) {
+                        timeout = true;
+                        break;
+                    }
+                    phase[0] ^= 1u;
+                    if (SPLIT && lane < nb_cur) {  // move staged sources into the group's frame
+                        const float4 sh = sm.shift[0][lane];
+                        float4* q = &sm.src[0][sm.pre[0][lane]];
+                        for (int kk = 0; kk < sm.cnt[0][lane]; ++kk) {
+                            float4 v = q[kk];
+                            v.x += sh.x;
+                            v.y += sh.y;
+                            v.z += sh.z;
+                            q[kk] = v;
                         }
                     }
-                    if (ns_cur > 0) {
-                        if (!mbar_wait(&sm.bar[bcur], phase[bcur])) {
-                            timeout = true;
-                            break;
-                        }
-                        phase[bcur] ^= 1u;
-                        if (SPLIT && lane < be) {  // move staged sources into the group's frame
-                            const float4 sh = sm.shift[bcur][lane];
-                            float4* q = &sm.src[bcur][sm.pre[bcur][lane]];
-                            for (int kk = 0; kk < sm.cnt[bcur][lane]; ++kk) {
-                                float4 v = q[kk];
-                                v.x += sh.x;
-                                v.y += sh.y;
-                                v.z += sh.z;
-                                q[kk] = v;
-                            }
-                        }
-                        __syncwarp();
-                        p2p_chunk<SPLIT, SOFT>(g, sm.src[bcur], ns_cur, wp.eps2, wp.ih);
-                        __syncwarp();
-                    }
+                    __syncwarp();
+                    p2p_chunk<SPLIT, SOFT>(g, sm.src[0], ns_cur, wp.eps2, wp.ih);
+                    __syncwarp();
                     total += ns_cur;
-                    if (kBuffers == 1 && k + 1 < nbatch) {
-                        // single buffer: stage the next batch (its info is in
-                        // registers) and fetch the info of the one after
-                        ns_next = stage_batch(sm, 0, info, lane, src);
-                        const int i2 = (k + 2) * be;
-                        if (k + 2 < nbatch) {
-                            if ((i2 & (kListChunk - 1)) == 0) chunk_pf = LB.near_next[chunk_pf];
-                            info = load_near_info<SPLIT>(T, LB, chunk_pf, i2 + lane, lane < be && i2 + lane < nnear,
-                                                         gchi, gclo);
+                    // stage the next batch (its info is in registers), then fetch
+                    // the info of the one after
+                    int ns_next = 0;
+                    if (pos < nnear) {
+                        ns_next = stage_fitting(sm, info, lane, src, tile, nb);
+                        nb_cur = nb;
+                        pos += nb;
+                        if (pos < nnear) {
+                            if ((pos & (kListChunk - 1)) < nb) chunk = LB.near_next[chunk];
+                            info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
                         }
                     }
                     ns_cur = ns_next;
