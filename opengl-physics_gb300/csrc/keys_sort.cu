@@ -210,16 +210,31 @@ void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s
 // 63-bit keys by the reference's FP64 centre recurrence
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ long long ordered_bits(double x) {
+    // Integer image of a finite double that orders like the double (-0
+    // taken as +0): one 64-bit compare replaces the FP64 comparison.
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+
 template <int LEVELS>
 __device__ __forceinline__ unsigned axis_bits(double p, double c, double h) {
-    // Returns LEVELS octant bits of one axis, level 0 in the highest bit.
+    // Returns LEVELS octant bits of one axis, level 0 in the highest bit:
+    // bit = p >= c, then h = h / 2 and c = c +- h rounded in FP64 (NewChild).
+    // GB300's FP64 pipe is narrow, so only the centre add stays FP64: the
+    // comparison is an integer compare of ordered bit images, the halving an
+    // exponent decrement (exact: h >= 1e-12 stays normal over 21 levels) and
+    // c - h the addition of -h (the same IEEE result).
+    const long long op = ordered_bits(p);
+    long long hb = __double_as_longlong(h);
     unsigned bits = 0;
 #pragma unroll
     for (int l = 0; l < LEVELS; ++l) {
-        const bool b = p >= c;
+        const bool b = op >= ordered_bits(c);
         bits = (bits << 1) | (b ? 1u : 0u);
-        h = __dmul_rn(0.5, h);
-        c = b ? __dadd_rn(c, h) : __dsub_rn(c, h);
+        hb -= 1ll << 52;
+        c = __dadd_rn(c, __longlong_as_double(b ? hb : (hb | (long long)0x8000000000000000ull)));
     }
     return bits;
 }

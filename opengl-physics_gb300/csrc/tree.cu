@@ -237,63 +237,129 @@ __device__ __forceinline__ void write_walk_record(NodeArrays& T, int node, doubl
 // Leaf moments, plus the group acceleration scale amin[leaf] = min over the
 // members of |a| from `acc` (the accelerations carried into this tree order;
 // zero before the first evaluation) that the learned opening test reads.
+//
+// GB300's FP64 pipe runs at 1/32 of the FP32 rate, so the per-particle work
+// is FP32: each member's offset from the leaf centre is a double-float pair
+// (error-free differences of the double-float position and centre), mass
+// and first moment are summed as double-float pairs with exact products,
+// and only the per-leaf results are FP64.  maxRadius keeps the reference's
+// FP64 value: the members within FP32 rounding of the FP32 maximum distance
+// are re-measured in FP64 (Tree.cpp:188-201).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    e = b - (s - a);
+}
+
+// Offset of a double-float coordinate (h + l) from a double-float centre
+// (ch + cl), as a normalised double-float pair.
+__device__ __forceinline__ void df_offset(float h, float l, float ch, float cl, float& oh, float& ol) {
+    float s, e;
+    two_sum(h, -ch, s, e);
+    fast_two_sum(s, e + (l - cl), oh, ol);
+}
+
+// (Sh, Sl) += m * (oh + ol), the product of the high parts exact.
+__device__ __forceinline__ void df_add_prod(float& Sh, float& Sl, float m, float oh, float ol) {
+    const float p = m * oh;
+    const float pe = fmaf(m, oh, -p) + m * ol;
+    float t, e;
+    two_sum(Sh, p, t, e);
+    fast_two_sum(t, Sl + (e + pe), Sh, Sl);
+}
+
 __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C, const float4* __restrict__ pos,
                                                       const float4* __restrict__ plo, float4* __restrict__ src,
                                                       const float4* __restrict__ acc,
                                                       const int* __restrict__ leaf_list, int split, int quadrupole) {
     const int nleaves = C->nleaves;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int li = blockIdx.x * blockDim.x + threadIdx.x; li < nleaves; li += gridDim.x * blockDim.x) {
         const int leaf = leaf_list[li];
         const int s = T.start[leaf], cnt = T.count[leaf];
-        double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+        const double ccx = T.cx[leaf], ccy = T.cy[leaf], ccz = T.cz[leaf];
+        const float chx = (float)ccx, chy = (float)ccy, chz = (float)ccz;
+        const float clx = (float)(ccx - (double)chx), cly = (float)(ccy - (double)chy),
+                    clz = (float)(ccz - (double)chz);
+        // pass 1: mass and first moment about the leaf centre
+        float Mh = 0.f, Ml = 0.f, Xh = 0.f, Xl = 0.f, Yh = 0.f, Yl = 0.f, Zh = 0.f, Zl = 0.f;
         for (int j = s; j < s + cnt; ++j) {
             const float4 p = pos[j];
-            double x = p.x, y = p.y, z = p.z;
-            if (plo) {
-                const float4 q = plo[j];
-                x += (double)q.x;
-                y += (double)q.y;
-                z += (double)q.z;
-            }
-            const double m = p.w;
-            M += m;
-            Sx = fma(m, x, Sx);
-            Sy = fma(m, y, Sy);
-            Sz = fma(m, z, Sz);
+            const float4 q = plo ? plo[j] : zero4;
+            float ox, oxl, oy, oyl, oz, ozl;
+            df_offset(p.x, q.x, chx, clx, ox, oxl);
+            df_offset(p.y, q.y, chy, cly, oy, oyl);
+            df_offset(p.z, q.z, chz, clz, oz, ozl);
+            float t, e;
+            two_sum(Mh, p.w, t, e);
+            fast_two_sum(t, Ml + e, Mh, Ml);
+            df_add_prod(Xh, Xl, p.w, ox, oxl);
+            df_add_prod(Yh, Yl, p.w, oy, oyl);
+            df_add_prod(Zh, Zl, p.w, oz, ozl);
         }
-        const double ccx = T.cx[leaf], ccy = T.cy[leaf], ccz = T.cz[leaf];
-        double cx = ccx, cy = ccy, cz = ccz;
+        const double M = (double)Mh + (double)Ml;
+        double ocx = 0.0, ocy = 0.0, ocz = 0.0;  // COM - centre
         if (M > 0.0) {
             const double inv = 1.0 / M;
-            cx = Sx * inv;
-            cy = Sy * inv;
-            cz = Sz * inv;
+            ocx = ((double)Xh + (double)Xl) * inv;
+            ocy = ((double)Yh + (double)Yl) * inv;
+            ocz = ((double)Zh + (double)Zl) * inv;
         }
-        double maxr2 = 0.0;
+        const double cx = ccx + ocx, cy = ccy + ocy, cz = ccz + ocz;
+        const float ohx = (float)ocx, ohy = (float)ocy, ohz = (float)ocz;
+        const float olx = (float)(ocx - (double)ohx), oly = (float)(ocy - (double)ohy),
+                    olz = (float)(ocz - (double)ohz);
+        // pass 2: FP32 distances from the COM, quadrupole, amin, walk sources
+        float maxf = 0.f;
         float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f, q4 = 0.f;
         float amin2 = 3.0e38f;
-        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int j = s; j < s + cnt; ++j) {
             const float4 p = pos[j];
             const float4 a = acc[j];
             amin2 = fminf(amin2, a.x * a.x + a.y * a.y + a.z * a.z);
             const float4 l = plo ? plo[j] : zero4;
-            const double x = (double)p.x + (double)l.x, y = (double)p.y + (double)l.y, z = (double)p.z + (double)l.z;
-            const double dx = x - cx, dy = y - cy, dz = z - cz;
-            maxr2 = fmax(maxr2, dx * dx + dy * dy + dz * dz);
+            float ox, oxl, oy, oyl, oz, ozl;
+            df_offset(p.x, l.x, chx, clx, ox, oxl);
+            df_offset(p.y, l.y, chy, cly, oy, oyl);
+            df_offset(p.z, l.z, chz, clz, oz, ozl);
+            const float fx = (ox - ohx) + (oxl - olx), fy = (oy - ohy) + (oyl - oly), fz = (oz - ohz) + (ozl - olz);
+            const float d2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+            maxf = fmaxf(maxf, d2);
             if (quadrupole && cnt > 1) {
-                const float fx = (float)dx, fy = (float)dy, fz = (float)dz, m = p.w;
-                const float d2 = fx * fx + fy * fy + fz * fz;
+                const float m = p.w;
                 q0 += m * (3.f * fx * fx - d2);
                 q1 += m * (3.f * fy * fy - d2);
                 q2 += m * 3.f * fx * fy;
                 q3 += m * 3.f * fx * fz;
                 q4 += m * 3.f * fy * fz;
             }
-            if (split)
-                src[j] = make_float4((float)(x - ccx), (float)(y - ccy), (float)(z - ccz), p.w);
-            else
-                src[j] = p;
+            src[j] = split ? make_float4(ox + oxl, oy + oyl, oz + ozl, p.w) : p;
+        }
+        // pass 3: the FP64 maximum over the members that can hold it.  An FP32
+        // distance is within a few ulps of the leaf's half size of the FP64
+        // one, so no member farther than the cut can be missed.
+        double maxr2 = 0.0;
+        const float rcut = sqrtf(maxf) * (1.f - 4e-6f) - 2e-6f * (float)T.half[leaf];
+        const float cut = rcut > 0.f ? rcut * rcut : -1.f;
+        for (int j = s; j < s + cnt; ++j) {
+            const float4 p = pos[j];
+            const float4 l = plo ? plo[j] : zero4;
+            float ox, oxl, oy, oyl, oz, ozl;
+            df_offset(p.x, l.x, chx, clx, ox, oxl);
+            df_offset(p.y, l.y, chy, cly, oy, oyl);
+            df_offset(p.z, l.z, chz, clz, oz, ozl);
+            const float fx = (ox - ohx) + (oxl - olx), fy = (oy - ohy) + (oyl - oly), fz = (oz - ohz) + (ozl - olz);
+            if (fmaf(fx, fx, fmaf(fy, fy, fz * fz)) >= cut) {
+                const double x = (double)p.x + (double)l.x, y = (double)p.y + (double)l.y,
+                             z = (double)p.z + (double)l.z;
+                const double dx = x - cx, dy = y - cy, dz = z - cz;
+                maxr2 = fmax(maxr2, dx * dx + dy * dy + dz * dz);
+            }
         }
         const double maxr = sqrt(maxr2);
         const double Q[5] = {q0, q1, q2, q3, q4};
@@ -306,9 +372,8 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
         for (int k = 0; k < 5; ++k) T.quad[5 * leaf + k] = Q[k];
         const int level = T.level[leaf];
         write_walk_record(T, leaf, M, cx, cy, cz, Q, maxr, true, s, cnt, level);
-        const float hx = (float)ccx, hy = (float)ccy, hz = (float)ccz;
-        T.chi[leaf] = make_float4(hx, hy, hz, 0.f);
-        T.clo[leaf] = make_float4((float)(ccx - (double)hx), (float)(ccy - (double)hy), (float)(ccz - (double)hz), 0.f);
+        T.chi[leaf] = make_float4(chx, chy, chz, 0.f);
+        T.clo[leaf] = make_float4(clx, cly, clz, 0.f);
     }
 }
 
