@@ -70,10 +70,13 @@ __device__ __forceinline__ int digit_lower_bound(const unsigned long long* __res
 
 constexpr int kLevelThreads = 256;
 
-// One level of the split.  Ensemble (F.sys_levels > 0): levels above
-// sys_levels group systems by id digits, always split and carry no geometry;
-// a child at level sys_levels is a system root and takes that system's cube;
-// below it the reference's recurrence runs from that root.
+// One level of the split, eight lanes per node: lane d finds where octant d
+// begins in the node's key range (d = 1..7 by independent binary searches,
+// so the top levels' long ranges cost one search's latency, not seven) and
+// creates child d.  Ensemble (F.sys_levels > 0): levels above sys_levels
+// group systems by id digits, always split and carry no geometry; a child at
+// level sys_levels is a system root and takes that system's cube; below it
+// the reference's recurrence runs from that root.
 __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T, Counters* C,
                                                                    const unsigned long long* __restrict__ keys,
                                                                    int l, int leaf_cap, int max_depth, Forest F) {
@@ -83,36 +86,41 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
     const bool virt = l < F.sys_levels;                 // this level groups systems
     const bool sys_child = l + 1 == F.sys_levels;      // children are system roots
     const int depth_cap = max_depth + F.sys_levels;    // max_depth counts from each system root
-    for (int node = begin + blockIdx.x * blockDim.x + threadIdx.x; node < end; node += gridDim.x * blockDim.x) {
-        const int cnt = T.count[node];
-        if (!virt && !(cnt > leaf_cap && l < depth_cap)) continue;  // stays a leaf
-        const int s = T.start[node];
-        const int e = s + cnt;
-        int bnd[9];
-        bnd[0] = s;
-        bnd[8] = e;
-        int lo = s;
-#pragma unroll
-        for (unsigned d = 1; d < 8; ++d) {
-            lo = digit_lower_bound(keys, lo, e, shift, d);
-            bnd[d] = lo;
+    const int lane = threadIdx.x & 31;
+    const int d = lane & 7;
+    const unsigned gmask = 0xFFu << (lane & 24);       // the node's eight lanes
+    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 3;
+    const long long ngroups = (gridDim.x * (long long)blockDim.x) >> 3;
+    // every lane of a warp runs the same number of iterations (shuffles below)
+    const int span = end - begin;
+    const long long warp0 = gid & ~3ll;
+    for (long long g0 = warp0; g0 < span; g0 += ngroups) {
+        const int node = begin + (int)(g0 + (gid & 3));
+        bool split = false;
+        int s = 0, cnt = 0;
+        if (node < end) {
+            cnt = T.count[node];
+            split = virt || (cnt > leaf_cap && l < depth_cap);  // else it stays a leaf
+            s = T.start[node];
         }
-        int nch = 0;
-#pragma unroll
-        for (int d = 0; d < 8; ++d) nch += bnd[d + 1] > bnd[d];
-        const int base = atomicAdd(&C->next_free, nch);
+        const int e = s + cnt;
+        const int bd = split ? (d == 0 ? s : digit_lower_bound(keys, s, e, shift, (unsigned)d)) : 0;
+        int bn = __shfl_down_sync(0xffffffffu, bd, 1, 8);  // where octant d + 1 begins
+        if (d == 7) bn = e;
+        const bool has = split && bn > bd;
+        const unsigned hm = (__ballot_sync(0xffffffffu, has) & gmask) >> (lane & 24);
+        const int nch = __popc(hm);
+        int base = 0;
+        if (split && d == 0) base = atomicAdd(&C->next_free, nch);
+        base = __shfl_sync(0xffffffffu, base, lane & 24, 32);
+        if (!split) continue;
         if (base + nch > T.cap) {
-            atomicOr(&C->status, kStNodeOverflow);
+            if (d == 0) atomicOr(&C->status, kStNodeOverflow);
             continue;
         }
-        const double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
-        const double child_half = 0.5 * T.half[node];
-        const int proot = T.sysroot[node];
-        int c = base;
-#pragma unroll
-        for (int d = 0; d < 8; ++d) {
-            const int cs = bnd[d], ce = bnd[d + 1];
-            if (ce <= cs) continue;
+        if (has) {
+            const int c = base + __popc(hm & ((1u << d) - 1u));
+            const int cs = bd, ce = bn;
             T.start[c] = cs;
             T.count[c] = ce - cs;
             T.first_child[c] = -1;
@@ -133,21 +141,24 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
                 }
                 T.sysroot[c] = c;
             } else {
+                const double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
+                const double child_half = 0.5 * T.half[node];
                 T.cx[c] = (d & 1) ? __dadd_rn(pcx, child_half) : __dsub_rn(pcx, child_half);
                 T.cy[c] = (d & 2) ? __dadd_rn(pcy, child_half) : __dsub_rn(pcy, child_half);
                 T.cz[c] = (d & 4) ? __dadd_rn(pcz, child_half) : __dsub_rn(pcz, child_half);
                 T.half[c] = child_half;
-                T.sysroot[c] = proot;
+                T.sysroot[c] = T.sysroot[node];
             }
             if (l + 1 >= kKeyLevels && ce - cs > leaf_cap && l + 1 < depth_cap) {
                 atomicOr(&C->status, kStDepthLimit);
                 atomicAdd(&C->depth_limited, 1);
             }
-            ++c;
         }
-        T.first_child[node] = base;
-        T.nchild[node] = (unsigned char)nch;
-        atomicMax(&C->levels_used, l + 1);
+        if (d == 0) {
+            T.first_child[node] = base;
+            T.nchild[node] = (unsigned char)nch;
+            atomicMax(&C->levels_used, l + 1);
+        }
     }
     // The last block to finish publishes where level l+2 begins.
     __syncthreads();
@@ -167,8 +178,8 @@ void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* ke
                         int max_depth, const Forest& F, cudaStream_t s) {
     // Enough threads for the widest level (nodes <= cap); levels above it
     // exit after a bounds check.
-    long long blocks = ((long long)T.cap / 4 + kLevelThreads - 1) / kLevelThreads;
-    if (blocks > 152 * 4) blocks = 152 * 4;
+    long long blocks = ((long long)T.cap / 4 * 8 + kLevelThreads - 1) / kLevelThreads;
+    if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks < 1) blocks = 1;
     for (int l = 0; l < kKeyLevels; ++l)
         tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth, F);
