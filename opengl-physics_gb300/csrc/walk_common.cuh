@@ -71,4 +71,44 @@ __device__ __forceinline__ void list_append(ChunkList& L, bool has, int val, int
     L.count += k;
 }
 
+// Two candidates per lane (v0 then v1), appended as one batch of up to 64:
+// all v0 in lane order, then all v1.  One chunk-boundary check for both.
+__device__ __forceinline__ void list_append2(ChunkList& L, bool has0, int v0, bool has1, int v1,
+                                             int* __restrict__ pool, int* __restrict__ next, int* counter, int cap,
+                                             int lane, unsigned lt_mask, unsigned& bad) {
+    const unsigned m0 = __ballot_sync(0xffffffffu, has0);
+    const unsigned m1 = __ballot_sync(0xffffffffu, has1);
+    const int k0 = __popc(m0);
+    const int k = k0 + __popc(m1);
+    if (k == 0) return;
+    if (L.cur < 0) {
+        L.cur = L.first = alloc_chunk(L, counter, lane);
+        L.pos = 0;
+    }
+    int newc = -1;
+    if (L.pos + k > kListChunk) {  // k <= 64 < kListChunk: at most one new chunk
+        newc = alloc_chunk(L, counter, lane);
+        if (lane == 0 && L.cur < cap) next[L.cur] = newc;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        if (q == 0 ? has0 : has1) {
+            const int i = L.pos + (q == 0 ? __popc(m0 & lt_mask) : k0 + __popc(m1 & lt_mask));
+            const int c = i < kListChunk ? L.cur : newc;
+            const int p = i < kListChunk ? i : i - kListChunk;
+            if (c < cap)
+                pool[(long long)c * kListChunk + p] = q == 0 ? v0 : v1;
+            else
+                bad |= kStListOverflow;
+        }
+    }
+    if (newc >= 0) {
+        L.cur = newc;
+        L.pos = L.pos + k - kListChunk;
+    } else {
+        L.pos += k;
+    }
+    L.count += k;
+}
+
 }  // namespace ngrav

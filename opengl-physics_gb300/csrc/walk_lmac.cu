@@ -260,28 +260,25 @@ __global__ void __launch_bounds__(kLwThreads, MINB) walk_lmac_round_kernel(NodeA
                     }
                 }
             }
+            tests += __popc(__ballot_sync(0xffffffffu, kind[0] >= 2)) + __popc(__ballot_sync(0xffffffffu, kind[1] >= 2));
+            list_append2(near, kind[0] == 1, node[0], kind[1] == 1, node[1], LB.near, LB.near_next, &C->near_chunks,
+                         LB.near_chunk_cap, lane, lt_mask, bad);
+            list_append2(far, kind[0] == 2, node[0], kind[1] == 2, node[1], LB.far, LB.far_next, &C->far_chunks,
+                         LB.far_chunk_cap, lane, lt_mask, bad);
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                tests += __popc(__ballot_sync(0xffffffffu, kind[q] >= 2));
-                list_append(near, kind[q] == 1, node[q], LB.near, LB.near_next, &C->near_chunks,
-                            LB.near_chunk_cap, lane, lt_mask, bad);
-                list_append(far, kind[q] == 2, node[q], LB.far, LB.far_next, &C->far_chunks, LB.far_chunk_cap,
-                            lane, lt_mask, bad);
+            for (int q = 0; q < 2; ++q)
                 pend_append(pend, kind[q] == 4, node[q], R, out, pend_ctr, leaf, lane, lt_mask, bad);
-            }
-            bool ovf = false;
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            {  // both nodes' children onto the stack with one scan
                 int tot;
-                const int off = warp_excl_scan(nch[q], lane, tot);
+                const int off = warp_excl_scan(nch[0] + nch[1], lane, tot);
                 if (size + tot > stack_cap) {
-                    ovf = true;
-                    break;
+                    bad |= kStStackOverflow;
+                } else {
+                    for (int c = 0; c < nch[0]; ++c) stack[size + off + c] = link[0] + c;
+                    for (int c = 0; c < nch[1]; ++c) stack[size + off + nch[0] + c] = link[1] + c;
+                    size += tot;
                 }
-                for (int c = 0; c < nch[q]; ++c) stack[size + off + c] = link[q] + c;
-                size += tot;
             }
-            if (ovf) bad |= kStStackOverflow;
             stack_max = max(stack_max, size);
             __syncwarp();
         }
