@@ -162,29 +162,23 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(NodeArrays T, Counte
                     }
                 }
             }
-#pragma unroll
-            for (int q = 0; q < kNPL; ++q) {
-                tests += __popc(__ballot_sync(0xffffffffu, tested_any[q]));
-                list_append(near, kind[q] == 1, node[q], LB.near, LB.near_next, &C->near_chunks,
-                            LB.near_chunk_cap, lane, lt_mask, bad);
-                list_append(far, kind[q] == 2, node[q], LB.far, LB.far_next, &C->far_chunks, LB.far_chunk_cap,
-                            lane, lt_mask, bad);
-            }
-            bool ovf = false;
-#pragma unroll
-            for (int q = 0; q < kNPL; ++q) {
+            static_assert(kNPL == 2, "the batched appends below take two nodes per lane");
+            tests += __popc(__ballot_sync(0xffffffffu, tested_any[0])) +
+                     __popc(__ballot_sync(0xffffffffu, tested_any[1]));
+            list_append2(near, kind[0] == 1, node[0], kind[1] == 1, node[1], LB.near, LB.near_next, &C->near_chunks,
+                         LB.near_chunk_cap, lane, lt_mask, bad);
+            list_append2(far, kind[0] == 2, node[0], kind[1] == 2, node[1], LB.far, LB.far_next, &C->far_chunks,
+                         LB.far_chunk_cap, lane, lt_mask, bad);
+            {  // both nodes' children onto the stack with one scan
                 int tot;
-                const int off = warp_excl_scan(nch[q], lane, tot);
+                const int off = warp_excl_scan(nch[0] + nch[1], lane, tot);
                 if (size + tot > stack_cap) {
-                    ovf = true;
+                    bad |= kStStackOverflow;
                     break;
                 }
-                for (int k = 0; k < nch[q]; ++k) stack[size + off + k] = link[q] + k;
+                for (int k = 0; k < nch[0]; ++k) stack[size + off + k] = link[0] + k;
+                for (int k = 0; k < nch[1]; ++k) stack[size + off + nch[0] + k] = link[1] + k;
                 size += tot;
-            }
-            if (ovf) {
-                bad |= kStStackOverflow;
-                break;
             }
             stack_max = max(stack_max, size);
             __syncwarp();
