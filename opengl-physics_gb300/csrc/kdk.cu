@@ -649,40 +649,49 @@ double run_fma_probe(int sm_count, cudaStream_t s) {
 // FP32 pairs, tiled: a block holds 256 targets (one per thread) and streams
 // one contiguous share of the sources through shared memory; each source tile
 // is summed in FP32 and added to the thread's FP64 totals.  Partial sums per
-// (share, target) are reduced in share order by sampler_reduce_kernel.
+// (share, target) are reduced in share order by sampler_reduce_kernel.  The
+// self pair needs no test: its separation is exactly zero, so it adds zero
+// (with eps > 0, and for the spline, whose factor is 0 at r = 0); only the
+// unsoftened Plummer form masks r = 0.
 constexpr int kSampTile = 256;
 
-template <int SOFT>
+template <int SOFT, bool SPLIT>
 __global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, const float4* __restrict__ pos,
                                                                  const float4* __restrict__ plo,
                                                                  const int* __restrict__ slots, int nslots,
                                                                  float eps2, float ih, long long share,
                                                                  double* __restrict__ partial) {
     __shared__ float4 sp[kSampTile];
-    __shared__ float4 sl[kSampTile];
+    __shared__ float4 sl[SPLIT ? kSampTile : 1];
     const int t = blockIdx.x * kSampTile + threadIdx.x;
     const bool valid = t < nslots;
     const int ti = valid ? slots[t] : -1;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 tp = valid ? pos[ti] : zero;
-    const float4 tl = (valid && plo) ? plo[ti] : zero;
+    const float4 tl = (valid && SPLIT) ? plo[ti] : zero;
+    const bool mask0 = SOFT == kSoftPlummer && !(eps2 > 0.f);
     const long long j0 = (long long)blockIdx.y * share;
     const long long j1 = j0 + share < n ? j0 + share : n;
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (long long base = j0; base < j1; base += kSampTile) {
         const long long j = base + threadIdx.x;
         sp[threadIdx.x] = j < j1 ? pos[j] : zero;
-        sl[threadIdx.x] = (j < j1 && plo) ? plo[j] : zero;
+        if (SPLIT) sl[threadIdx.x] = j < j1 ? plo[j] : zero;
         __syncthreads();
         const int cnt = (int)(j1 - base < kSampTile ? j1 - base : kSampTile);
         float px = 0.f, py = 0.f, pz = 0.f;
         for (int k = 0; k < cnt; ++k) {
             const float4 p = sp[k];
-            const float4 l = sl[k];
-            const float dx = (p.x - tp.x) + (l.x - tl.x);
-            const float dy = (p.y - tp.y) + (l.y - tl.y);
-            const float dz = (p.z - tp.z) + (l.z - tl.z);
-            const float f = base + k == ti ? 0.f : pair_factor<SOFT>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), p.w, eps2, ih);
+            float dx = p.x - tp.x, dy = p.y - tp.y, dz = p.z - tp.z;
+            if (SPLIT) {
+                const float4 l = sl[k];
+                dx += l.x - tl.x;
+                dy += l.y - tl.y;
+                dz += l.z - tl.z;
+            }
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            float f = pair_factor<SOFT>(r2, p.w, eps2, ih);
+            if (mask0) f = r2 > 0.f ? f : 0.f;
             px = fmaf(f, dx, px);
             py = fmaf(f, dy, py);
             pz = fmaf(f, dz, pz);
@@ -727,12 +736,22 @@ void launch_sampler(long long n, const Particles& P, bool split, const int* slot
     long long share = (n + shares - 1) / shares;
     share = (share + kSampTile - 1) / kSampTile * kSampTile;
     const dim3 grid((nslots + kSampTile - 1) / kSampTile, shares);
-    if (spline_h > 0.0)
-        sampler_tiled_kernel<kSoftSpline><<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots,
-                                                                    0.f, (float)(1.0 / spline_h), share, partial);
-    else
-        sampler_tiled_kernel<kSoftPlummer><<<grid, kSampTile, 0, s>>>(n, P.pos, split ? P.plo : nullptr, slots, nslots,
-                                                                     (float)eps2, 0.f, share, partial);
+    const float ih = spline_h > 0.0 ? (float)(1.0 / spline_h) : 0.f;
+    if (spline_h > 0.0) {
+        if (split)
+            sampler_tiled_kernel<kSoftSpline, true><<<grid, kSampTile, 0, s>>>(n, P.pos, P.plo, slots, nslots, 0.f, ih,
+                                                                              share, partial);
+        else
+            sampler_tiled_kernel<kSoftSpline, false><<<grid, kSampTile, 0, s>>>(n, P.pos, nullptr, slots, nslots, 0.f,
+                                                                               ih, share, partial);
+    } else {
+        if (split)
+            sampler_tiled_kernel<kSoftPlummer, true><<<grid, kSampTile, 0, s>>>(n, P.pos, P.plo, slots, nslots,
+                                                                                (float)eps2, 0.f, share, partial);
+        else
+            sampler_tiled_kernel<kSoftPlummer, false><<<grid, kSampTile, 0, s>>>(n, P.pos, nullptr, slots, nslots,
+                                                                                 (float)eps2, 0.f, share, partial);
+    }
     sampler_reduce_kernel<<<(3 * nslots + 255) / 256, 256, 0, s>>>(partial, nslots, shares, out);
 }
 

@@ -419,7 +419,7 @@ int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o) {
     o->check_targets = 4096;
     o->revert_rms = 1e-3;
     o->rounds = 3;
-    o->screen = 100.0;
+    o->screen = 300.0;
     return NGRAV_OK;
 }
 
