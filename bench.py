@@ -226,7 +226,7 @@ def run_reference(args, rank, world):
 
 
 THETA_GRID = (0.5, 0.55, 0.6, 0.625, 0.65, 0.675, 0.7, 0.75, 0.8)
-BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 3e-4, 4e-4, 5e-4, 7e-4, 1e-3)
+BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 3e-4, 3.5e-4, 4e-4, 5e-4, 7e-4, 1e-3)
 TARGET_RMS = 1e-3
 
 
