@@ -139,6 +139,10 @@ typedef struct ngrav_gpu_stats {
     double lmac_last_check_rms;
     /* KDK steps launched as a captured CUDA graph: captures made, replays */
     long long graph_captures, graph_replays;
+    /* System::ParticleEvals (include/ngrav/System.hpp:115): accelerations
+     * computed, all particles per evaluation, the closing set per block-step
+     * substep; cumulative */
+    long long cum_particle_evals;
 } ngrav_gpu_stats;
 
 typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;

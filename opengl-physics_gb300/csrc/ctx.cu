@@ -53,8 +53,8 @@ bool split_of(const ngrav_gpu_ctx* ctx) { return ctx->opts.precision == NGRAV_PR
 
 void free_particles(ngrav_gpu_ctx* ctx) {
     Particles& P = ctx->P;
-    dfree(P.pos); dfree(P.plo); dfree(P.vel); dfree(P.acc); dfree(P.src); dfree(P.id);
-    dfree(P.pos2); dfree(P.plo2); dfree(P.vel2); dfree(P.acc2); dfree(P.id2);
+    dfree(P.pos); dfree(P.plo); dfree(P.vel); dfree(P.vlo); dfree(P.acc); dfree(P.src); dfree(P.id);
+    dfree(P.pos2); dfree(P.plo2); dfree(P.vel2); dfree(P.vlo2); dfree(P.acc2); dfree(P.id2);
     P.cap = 0;
     SortBuffers& S = ctx->SB;
     dfree(S.keys); dfree(S.keys_alt); dfree(S.vals); dfree(S.vals_alt); dfree(S.hist); dfree(S.scan_tmp);
@@ -79,6 +79,7 @@ int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
     const long long c = n;
     Particles& P = ctx->P;
     NG_CUDA(dalloc(P.pos, c)); NG_CUDA(dalloc(P.plo, c)); NG_CUDA(dalloc(P.vel, c)); NG_CUDA(dalloc(P.acc, c));
+    NG_CUDA(dalloc(P.vlo, c)); NG_CUDA(dalloc(P.vlo2, c));
     NG_CUDA(dalloc(P.src, c)); NG_CUDA(dalloc(P.id, c));
     NG_CUDA(dalloc(P.pos2, c)); NG_CUDA(dalloc(P.plo2, c)); NG_CUDA(dalloc(P.vel2, c)); NG_CUDA(dalloc(P.acc2, c));
     NG_CUDA(dalloc(P.id2, c));
@@ -219,6 +220,7 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     std::swap(P.pos, P.pos2);
     std::swap(P.plo, P.plo2);
     std::swap(P.vel, P.vel2);
+    std::swap(P.vlo, P.vlo2);
     std::swap(P.acc, P.acc2);
     std::swap(P.id, P.id2);
     rec(ctx, 2);
@@ -314,6 +316,7 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
                             ctx->phase_ms[4] + ctx->phase_ms[5];
     }
     ctx->force_evals += 1;
+    ctx->cum_particle_evals += ctx->block_on ? (long long)ctx->hc.targets : ctx->n;
     ctx->acc_valid = true;
     ctx->cum_evals += 1;
     ctx->cum_pairs += (long long)ctx->hc.p2p_pairs;
@@ -461,6 +464,7 @@ bool enqueue_step_graph(ngrav_gpu_ctx* ctx, float hdt, float fdt) {
             std::swap(ctx->P.pos, ctx->P.pos2);
             std::swap(ctx->P.plo, ctx->P.plo2);
             std::swap(ctx->P.vel, ctx->P.vel2);
+            std::swap(ctx->P.vlo, ctx->P.vlo2);
             std::swap(ctx->P.acc, ctx->P.acc2);
             std::swap(ctx->P.id, ctx->P.id2);
             ctx->launches += g.launches;
@@ -634,10 +638,13 @@ int ngrav_gpu_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* opts) {
     if (prec_change && ctx->have) {
         // PLAIN -> SPLIT starts with lo = 0; SPLIT -> PLAIN rounds hi + lo to FP32.
         NG_CUDA(cudaSetDevice(ctx->opts.device));
-        if (opts->precision == NGRAV_PRECISION_SPLIT)
+        if (opts->precision == NGRAV_PRECISION_SPLIT) {
             NG_CUDA(cudaMemsetAsync(ctx->P.plo, 0, sizeof(float4) * ctx->n, ctx->stream));
-        else
+            NG_CUDA(cudaMemsetAsync(ctx->P.vlo, 0, sizeof(float4) * ctx->n, ctx->stream));
+        } else {
             launch_collapse_split(ctx->P.pos, ctx->P.plo, ctx->n, ctx->stream);
+            launch_collapse_split(ctx->P.vel, ctx->P.vlo, ctx->n, ctx->stream);  // keeps vel.w (the rung)
+        }
         NG_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     ctx->opts = *opts;
@@ -819,7 +826,8 @@ int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, dou
     double* st = ctx->stage;
     launch_download(n, ctx->P.id, ctx->P.pos, split_of(ctx) ? ctx->P.plo : nullptr, st, st + n, st + 2 * n,
                     ctx->stream);
-    launch_download(n, ctx->P.id, ctx->P.vel, nullptr, st + 3 * n, st + 4 * n, st + 5 * n, ctx->stream);
+    launch_download(n, ctx->P.id, ctx->P.vel, split_of(ctx) ? ctx->P.vlo : nullptr, st + 3 * n, st + 4 * n, st + 5 * n,
+                    ctx->stream);
     double* outs[6] = {x, y, z, vx, vy, vz};
     for (int k = 0; k < 6; ++k)
         if (outs[k])
@@ -835,6 +843,7 @@ int ngrav_gpu_get_frame_f32(ngrav_gpu_ctx* ctx, float* pos, float* vel) {
     const long long n = ctx->n;
     float* st = reinterpret_cast<float*>(ctx->stage);  // 7n doubles hold the 6n floats
     launch_frame_download(n, ctx->P.id, ctx->P.pos, split_of(ctx) ? ctx->P.plo : nullptr, ctx->P.vel,
+                          split_of(ctx) ? ctx->P.vlo : nullptr,
                           pos ? st : nullptr, vel ? st + 3 * n : nullptr, ctx->stream);
     if (pos) NG_CUDA(cudaMemcpyAsync(pos, st, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (vel) NG_CUDA(cudaMemcpyAsync(vel, st + 3 * n, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -999,6 +1008,7 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->ms_sort = ctx->phase_ms[1];
     out->ms_build = ctx->phase_ms[2];
     out->ms_moments = ctx->phase_ms[3];
+    out->cum_particle_evals = ctx->cum_particle_evals;
     out->ms_walk = ctx->phase_ms[4];
     out->ms_force = ctx->phase_ms[5];
     out->ms_total = ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] + ctx->phase_ms[4] +
@@ -1039,6 +1049,7 @@ int ngrav_gpu_reset_cumulative(ngrav_gpu_ctx* ctx) {
     ctx->launches = 0;
     ctx->cum_evals = ctx->cum_pairs = ctx->cum_p2c = 0;
     ctx->cum_ms_walk = ctx->cum_ms_force = ctx->cum_ms_eval = ctx->cum_ms_step = 0.0;
+    ctx->cum_particle_evals = 0;
     return NGRAV_OK;
 }
 

@@ -63,6 +63,7 @@ struct ngrav_gpu_ctx {
     double alpha = 0.001;             // relative opening test tolerance
     // block-timestep evaluation in progress: {finest substep, max rung}
     bool block_on = false;
+    long long cum_particle_evals = 0;  // System::ParticleEvals: targets of every evaluation
     int block_args[2] = {0, 0};
     double block_base = 0.0;
     // ensemble of independent systems (Forest of engine.cuh); nsys = 1: one system

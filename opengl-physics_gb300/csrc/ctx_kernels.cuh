@@ -57,7 +57,7 @@ void launch_walk_pp(const NodeArrays& T, Counters* C, const Particles& P, const 
                     int nwarps, cudaStream_t s);
 // kdk.cu: block timesteps
 void launch_frame_download(long long n, const int* id, const float4* pos, const float4* plo, const float4* vel,
-                           float* opos, float* ovel, cudaStream_t s);
+                           const float4* vlo, float* opos, float* ovel, cudaStream_t s);
 void launch_amax(long long n, const float4* acc, unsigned long long* out, cudaStream_t s);
 void launch_rung_download(long long n, const int* id, const float4* vel, int* out, cudaStream_t s);
 void launch_rungs(long long n, const Particles& P, double base, double eta, double eps, int max_rung, int* rmax,

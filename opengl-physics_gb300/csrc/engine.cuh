@@ -73,6 +73,7 @@ struct Counters {
     unsigned long long lm_fallbacks;
     unsigned long long lm_flushes;
     unsigned long long lm_screened;   // band pairs the error bound accepted without the network
+    unsigned long long targets;       // particles whose acceleration a block-step evaluation refreshed
 };
 
 // Per-group interaction lists written by the walk, read by the evaluation.
@@ -133,6 +134,7 @@ struct Particles {
     float4* pos = nullptr;
     float4* plo = nullptr;
     float4* vel = nullptr;
+    float4* vlo = nullptr;            // velocity low halves (SPLIT): kicks accumulate ~48 bits
     float4* acc = nullptr;
     float4* src = nullptr;
     int* id = nullptr;
@@ -140,6 +142,7 @@ struct Particles {
     float4* pos2 = nullptr;
     float4* plo2 = nullptr;
     float4* vel2 = nullptr;
+    float4* vlo2 = nullptr;
     float4* acc2 = nullptr;
     int* id2 = nullptr;
 };
@@ -200,6 +203,31 @@ struct Forest {
 };
 
 // System of a slot (binary search over the offsets).
+// (h, l) += d for a double-float pair: error-free two-sum, renormalised.
+__device__ __forceinline__ void df_add(float& h, float& l, float d) {
+    const float s = h + d;
+    const float bb = s - h;
+    const float e = (h - (s - bb)) + (d - bb);
+    const float l2 = l + e;
+    const float h2 = s + l2;
+    l = l2 - (h2 - s);
+    h = h2;
+}
+
+// Closing or opening half-kick of one particle: v += h a, as a double-float
+// pair when vl is given (split precision), else in FP32.
+__device__ __forceinline__ void kick_v(float4& v, float4* vl, float h, const float4& a) {
+    if (vl) {
+        df_add(v.x, vl->x, h * a.x);
+        df_add(v.y, vl->y, h * a.y);
+        df_add(v.z, vl->z, h * a.z);
+    } else {
+        v.x = fmaf(h, a.x, v.x);
+        v.y = fmaf(h, a.y, v.y);
+        v.z = fmaf(h, a.z, v.z);
+    }
+}
+
 __device__ __forceinline__ int forest_system(const Forest& F, long long k) {
     int lo = 0, hi = F.nsys - 1;
     while (lo < hi) {

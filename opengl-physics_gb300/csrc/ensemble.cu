@@ -79,7 +79,8 @@ __global__ void gather_float4_kernel(const float4* __restrict__ a, const int* __
 // part[8 nsys + 3 s ..].
 __global__ void __launch_bounds__(256) forest_diag_kernel(const float4* __restrict__ pos,
                                                           const float4* __restrict__ plo,
-                                                          const float4* __restrict__ vel, Forest F,
+                                                          const float4* __restrict__ vel,
+                                                          const float4* __restrict__ vlo, Forest F,
                                                           double* __restrict__ part) {
     __shared__ double red[8][8];
     __shared__ double com[3];
@@ -91,15 +92,17 @@ __global__ void __launch_bounds__(256) forest_diag_kernel(const float4* __restri
         const float4 p = pos[j];
         const float4 l = plo ? plo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 v = vel[j];
+        const float4 vl = vlo ? vlo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const double vx = (double)v.x + vl.x, vy = (double)v.y + vl.y, vz = (double)v.z + vl.z;
         const double m = p.w, x = (double)p.x + l.x, y = (double)p.y + l.y, z = (double)p.z + l.z;
         a[0] += m;
         a[1] += m * x;
         a[2] += m * y;
         a[3] += m * z;
-        a[4] += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
-        a[5] += m * v.x;
-        a[6] += m * v.y;
-        a[7] += m * v.z;
+        a[4] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        a[5] += m * vx;
+        a[6] += m * vy;
+        a[7] += m * vz;
     }
     for (int c = 0; c < 8; ++c) {
         for (int o = 16; o > 0; o >>= 1) a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
@@ -120,11 +123,13 @@ __global__ void __launch_bounds__(256) forest_diag_kernel(const float4* __restri
         const float4 p = pos[j];
         const float4 l = plo ? plo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 v = vel[j];
+        const float4 vl = vlo ? vlo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const double vx = (double)v.x + vl.x, vy = (double)v.y + vl.y, vz = (double)v.z + vl.z;
         const double m = p.w;
         const double dx = (double)p.x + l.x - cx, dy = (double)p.y + l.y - cy, dz = (double)p.z + l.z - cz;
-        L[0] += m * (dy * v.z - dz * v.y);
-        L[1] += m * (dz * v.x - dx * v.z);
-        L[2] += m * (dx * v.y - dy * v.x);
+        L[0] += m * (dy * vz - dz * vy);
+        L[1] += m * (dz * vx - dx * vz);
+        L[2] += m * (dx * vy - dy * vx);
     }
     __syncthreads();
     for (int c = 0; c < 3; ++c) {
@@ -183,7 +188,8 @@ void launch_forest_sampler(const Particles& P, bool split, const int* slots, int
 }
 
 void launch_forest_diag(const Particles& P, bool split, const Forest& F, double* part, cudaStream_t s) {
-    forest_diag_kernel<<<F.nsys, 256, 0, s>>>(P.pos, split ? P.plo : nullptr, P.vel, F, part);
+    forest_diag_kernel<<<F.nsys, 256, 0, s>>>(P.pos, split ? P.plo : nullptr, P.vel, split ? P.vlo : nullptr, F,
+                                              part);
 }
 
 void launch_forest_potential(const Particles& P, bool split, const Forest& F, double eps2, int chunks, double* part,

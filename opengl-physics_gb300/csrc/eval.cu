@@ -296,6 +296,7 @@ template <bool SPLIT, bool QUAD, int SOFT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
                                                             float4* __restrict__ acc, float4* __restrict__ vel,
+                                                            float4* __restrict__ vlo,
                                                             const int* __restrict__ leaf_list, WalkParams wp,
                                                             ListBuffers LB) {
     extern __shared__ __align__(128) unsigned char eval_smem_raw[];
@@ -493,10 +494,10 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                 acc[slot] = make_float4(ax, ay, az, 0.f);
                 if (wp.kick) {
                     float4 v = vel[slot];
-                    v.x = fmaf(wp.hdt, ax, v.x);
-                    v.y = fmaf(wp.hdt, ay, v.y);
-                    v.z = fmaf(wp.hdt, az, v.z);
+                    float4 vl = SPLIT ? vlo[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    kick_v(v, SPLIT ? &vl : nullptr, wp.hdt, make_float4(ax, ay, az, 0.f));
                     vel[slot] = v;
+                    if (SPLIT) vlo[slot] = vl;
                 }
             }
             __syncwarp();
@@ -544,7 +545,7 @@ void launch_eval(const NodeArrays& T, Counters* C, const Particles& P, const int
     const size_t smem = eval_smem_bytes();
 #define NGRAV_LAUNCH(SP, Q, Z)                                                                             \
     if (wp.split == (SP) && (wp.quadrupole != 0) == (Q) && soft == (Z))                                   \
-        eval_kernel<SP, Q, Z><<<blocks, kEvalThreads, smem, s>>>(T, C, P.src, P.acc, P.vel, leaf_list, wp, LB);
+        eval_kernel<SP, Q, Z><<<blocks, kEvalThreads, smem, s>>>(T, C, P.src, P.acc, P.vel, P.vlo, leaf_list, wp, LB);
     NGRAV_EVAL_INSTANCES(NGRAV_LAUNCH)
 #undef NGRAV_LAUNCH
 }

@@ -37,7 +37,11 @@ __global__ void upload_kernel(long long n, const T* __restrict__ x, const T* __r
         const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
         P.pos[i] = make_float4(hx, hy, hz, (float)m[i]);
         if (split) P.plo[i] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
-        P.vel[i] = vx ? make_float4((float)vx[i], (float)vy[i], (float)vz[i], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const double ux = vx ? (double)vx[i] : 0.0, uy = vx ? (double)vy[i] : 0.0, uz = vx ? (double)vz[i] : 0.0;
+        const float gx = (float)ux, gy = (float)uy, gz = (float)uz;
+        P.vel[i] = make_float4(gx, gy, gz, 0.f);
+        P.vlo[i] = split ? make_float4((float)(ux - (double)gx), (float)(uy - (double)gy), (float)(uz - (double)gz), 0.f)
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
         P.acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         P.id[i] = (int)i;
     }
@@ -56,7 +60,14 @@ __global__ void state_kernel(long long n, const T* __restrict__ x, const T* __re
         const float hx = (float)dx, hy = (float)dy, hz = (float)dz;
         P.pos[k] = make_float4(hx, hy, hz, P.pos[k].w);
         if (split) P.plo[k] = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz), 0.f);
-        if (vx) P.vel[k] = make_float4((float)vx[i], (float)vy[i], (float)vz[i], 0.f);
+        if (vx) {
+            const double ux = (double)vx[i], uy = (double)vy[i], uz = (double)vz[i];
+            const float gx = (float)ux, gy = (float)uy, gz = (float)uz;
+            P.vel[k] = make_float4(gx, gy, gz, 0.f);
+            P.vlo[k] = split ? make_float4((float)(ux - (double)gx), (float)(uy - (double)gy),
+                                           (float)(uz - (double)gz), 0.f)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 
@@ -119,7 +130,8 @@ void launch_download(long long n, const int* id, const float4* a, const float4* 
 // state value rounded once (the static_cast<float> of DeckSim::Snapshot).
 __global__ void frame_download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ pos,
                                       const float4* __restrict__ plo, const float4* __restrict__ vel,
-                                      float* __restrict__ opos, float* __restrict__ ovel) {
+                                      const float4* __restrict__ vlo, float* __restrict__ opos,
+                                      float* __restrict__ ovel) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
         const long long i = 3LL * id[k];
         if (opos) {
@@ -137,16 +149,23 @@ __global__ void frame_download_kernel(long long n, const int* __restrict__ id, c
         }
         if (ovel) {
             const float4 v = vel[k];
-            ovel[i + 0] = v.x;
-            ovel[i + 1] = v.y;
-            ovel[i + 2] = v.z;
+            if (vlo) {
+                const float4 l = vlo[k];
+                ovel[i + 0] = (float)((double)v.x + (double)l.x);
+                ovel[i + 1] = (float)((double)v.y + (double)l.y);
+                ovel[i + 2] = (float)((double)v.z + (double)l.z);
+            } else {
+                ovel[i + 0] = v.x;
+                ovel[i + 1] = v.y;
+                ovel[i + 2] = v.z;
+            }
         }
     }
 }
 
 void launch_frame_download(long long n, const int* id, const float4* pos, const float4* plo, const float4* vel,
-                           float* opos, float* ovel, cudaStream_t s) {
-    frame_download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, pos, plo, vel, opos, ovel);
+                           const float4* vlo, float* opos, float* ovel, cudaStream_t s) {
+    frame_download_kernel<<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, id, pos, plo, vel, vlo, opos, ovel);
 }
 
 __global__ void rung_download_kernel(long long n, const int* __restrict__ id, const float4* __restrict__ vel,
@@ -185,25 +204,25 @@ void launch_gather_slots(const int* inv, const int* targets, int nt, int* slots,
 template <bool SPLIT>
 __global__ void __launch_bounds__(256) kick_drift_kernel(long long n, float4* __restrict__ pos,
                                                          float4* __restrict__ plo, float4* __restrict__ vel,
-                                                         const float4* __restrict__ acc, float hdt, float dt,
-                                                         Counters* C) {
+                                                         float4* __restrict__ vlo, const float4* __restrict__ acc,
+                                                         float hdt, float dt, Counters* C) {
     double lo[3] = {1.0 / 0.0, 1.0 / 0.0, 1.0 / 0.0};
     double hi[3] = {-1.0 / 0.0, -1.0 / 0.0, -1.0 / 0.0};
     bool bad = false;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float4 v = vel[i];
+        float4 vl = SPLIT ? vlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 a = acc[i];
-        v.x = fmaf(hdt, a.x, v.x);
-        v.y = fmaf(hdt, a.y, v.y);
-        v.z = fmaf(hdt, a.z, v.z);
+        kick_v(v, SPLIT ? &vl : nullptr, hdt, a);
         vel[i] = v;
+        if (SPLIT) vlo[i] = vl;
         float4 p = pos[i];
         double q[3];
         if (SPLIT) {
             float4 l = plo[i];
             float* ph = &p.x;
             float* pl = &l.x;
-            const float dv[3] = {dt * v.x, dt * v.y, dt * v.z};
+            const float dv[3] = {fmaf(dt, v.x, dt * vl.x), fmaf(dt, v.y, dt * vl.y), fmaf(dt, v.z, dt * vl.z)};
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 // two-sum of hi + d, error folded into lo, then renormalised
@@ -265,9 +284,9 @@ void launch_kick_drift(const Particles& P, long long n, float hdt, float dt, boo
                        cudaStream_t s) {
     const unsigned b = grid_for(n, 256, 152 * 8);
     if (split)
-        kick_drift_kernel<true><<<b, 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.acc, hdt, dt, C);
+        kick_drift_kernel<true><<<b, 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.vlo, P.acc, hdt, dt, C);
     else
-        kick_drift_kernel<false><<<b, 256, 0, s>>>(n, P.pos, nullptr, P.vel, P.acc, hdt, dt, C);
+        kick_drift_kernel<false><<<b, 256, 0, s>>>(n, P.pos, nullptr, P.vel, nullptr, P.acc, hdt, dt, C);
 }
 
 // ---------------------------------------------------------------------------
@@ -289,8 +308,8 @@ __device__ __forceinline__ double block_sum_d(double v, double* sh) {
 }
 
 __device__ __forceinline__ void load_state_d(long long i, const float4* pos, const float4* plo, const float4* vel,
-                                             double& x, double& y, double& z, double& vx, double& vy, double& vz,
-                                             double& m) {
+                                             const float4* vlo, double& x, double& y, double& z, double& vx,
+                                             double& vy, double& vz, double& m) {
     const float4 p = pos[i];
     x = p.x;
     y = p.y;
@@ -306,17 +325,24 @@ __device__ __forceinline__ void load_state_d(long long i, const float4* pos, con
     vx = v.x;
     vy = v.y;
     vz = v.z;
+    if (vlo) {
+        const float4 l = vlo[i];
+        vx += (double)l.x;
+        vy += (double)l.y;
+        vz += (double)l.z;
+    }
 }
 
 // Pass 1: per block {M, Mx, My, Mz, KE, Px, Py, Pz}.
 __global__ void __launch_bounds__(kDiagThreads) diag_pass1_kernel(long long n, const float4* __restrict__ pos,
                                                                   const float4* __restrict__ plo,
                                                                   const float4* __restrict__ vel,
+                                                                  const float4* __restrict__ vlo,
                                                                   double* __restrict__ partial) {
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double x, y, z, vx, vy, vz, m;
-        load_state_d(i, pos, plo, vel, x, y, z, vx, vy, vz, m);
+        load_state_d(i, pos, plo, vel, vlo, x, y, z, vx, vy, vz, m);
         acc[0] += m;
         acc[1] += m * x;
         acc[2] += m * y;
@@ -336,12 +362,13 @@ __global__ void __launch_bounds__(kDiagThreads) diag_pass1_kernel(long long n, c
 // Pass 2: per block {Lx, Ly, Lz} about the given COM.
 __global__ void __launch_bounds__(kDiagThreads) diag_pass2_kernel(long long n, const float4* __restrict__ pos,
                                                                   const float4* __restrict__ plo,
-                                                                  const float4* __restrict__ vel, double cx,
+                                                                  const float4* __restrict__ vel,
+                                                                  const float4* __restrict__ vlo, double cx,
                                                                   double cy, double cz, double* __restrict__ partial) {
     double L[3] = {0, 0, 0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double x, y, z, vx, vy, vz, m;
-        load_state_d(i, pos, plo, vel, x, y, z, vx, vy, vz, m);
+        load_state_d(i, pos, plo, vel, vlo, x, y, z, vx, vy, vz, m);
         const double rx = x - cx, ry = y - cy, rz = z - cz;
         L[0] += m * (ry * vz - vy * rz);
         L[1] += m * (rz * vx - vz * rx);
@@ -357,12 +384,14 @@ __global__ void __launch_bounds__(kDiagThreads) diag_pass2_kernel(long long n, c
 int diag_blocks(long long n) { return (int)grid_for(n, kDiagThreads, 152 * 2); }
 
 void launch_diag_pass1(long long n, const Particles& P, bool split, double* partial, cudaStream_t s) {
-    diag_pass1_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel, partial);
+    diag_pass1_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel,
+                                                               split ? P.vlo : nullptr, partial);
 }
 
 void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, double cy, double cz, double* partial,
                        cudaStream_t s) {
-    diag_pass2_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel, cx, cy, cz,
+    diag_pass2_kernel<<<diag_blocks(n), kDiagThreads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, P.vel,
+                                                               split ? P.vlo : nullptr, cx, cy, cz,
                                                               partial);
 }
 
@@ -489,26 +518,27 @@ void launch_amax(long long n, const float4* acc, unsigned long long* out, cudaSt
 template <bool SPLIT>
 __global__ void __launch_bounds__(256) block_kick_drift_kernel(long long n, float4* __restrict__ pos,
                                                                float4* __restrict__ plo, float4* __restrict__ vel,
+                                                               float4* __restrict__ vlo,
                                                                const float4* __restrict__ acc, double base, int sub,
                                                                int rmax, float dtmin) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float4 v = vel[i];
+        float4 vl = SPLIT ? vlo[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const int rung = (int)v.w;
         const int units = 1 << (rmax - rung);
         if (sub % units == 0) {
             const float h = (float)(0.5 * base / (double)(1 << rung));
-            const float4 a = acc[i];
-            v.x = fmaf(h, a.x, v.x);
-            v.y = fmaf(h, a.y, v.y);
-            v.z = fmaf(h, a.z, v.z);
+            kick_v(v, SPLIT ? &vl : nullptr, h, acc[i]);
             vel[i] = v;
+            if (SPLIT) vlo[i] = vl;
         }
         float4 p = pos[i];
         if (SPLIT) {
             float4 l = plo[i];
             float* ph = &p.x;
             float* pl = &l.x;
-            const float dv[3] = {dtmin * v.x, dtmin * v.y, dtmin * v.z};
+            const float dv[3] = {fmaf(dtmin, v.x, dtmin * vl.x), fmaf(dtmin, v.y, dtmin * vl.y),
+                                 fmaf(dtmin, v.z, dtmin * vl.z)};
 #pragma unroll
             for (int k = 0; k < 3; ++k) {  // (hi, lo) += d with an error-free two-sum
                 const float s = ph[k] + dv[k];
@@ -537,11 +567,11 @@ void launch_rungs(long long n, const Particles& P, double base, double eta, doub
 void launch_block_kick_drift(long long n, const Particles& P, bool split, double base, int sub, int rmax, float dtmin,
                              cudaStream_t s) {
     if (split)
-        block_kick_drift_kernel<true><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.acc, base,
-                                                                                 sub, rmax, dtmin);
+        block_kick_drift_kernel<true><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, P.plo, P.vel, P.vlo,
+                                                                                 P.acc, base, sub, rmax, dtmin);
     else
-        block_kick_drift_kernel<false><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, nullptr, P.vel, P.acc,
-                                                                                  base, sub, rmax, dtmin);
+        block_kick_drift_kernel<false><<<grid_for(n, 256, 152 * 16), 256, 0, s>>>(n, P.pos, nullptr, P.vel, nullptr,
+                                                                                  P.acc, base, sub, rmax, dtmin);
 }
 
 // ---------------------------------------------------------------------------

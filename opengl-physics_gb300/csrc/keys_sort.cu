@@ -560,15 +560,18 @@ void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s) 
 
 __global__ void __launch_bounds__(256) permute_kernel(const unsigned* __restrict__ perm, long long n,
                                                       const float4* __restrict__ pos, const float4* __restrict__ plo,
-                                                      const float4* __restrict__ vel, const float4* __restrict__ acc,
+                                                      const float4* __restrict__ vel, const float4* __restrict__ vlo,
+                                                      const float4* __restrict__ acc,
                                                       const int* __restrict__ id, float4* __restrict__ pos2,
                                                       float4* __restrict__ plo2, float4* __restrict__ vel2,
-                                                      float4* __restrict__ acc2, int* __restrict__ id2) {
+                                                      float4* __restrict__ vlo2, float4* __restrict__ acc2,
+                                                      int* __restrict__ id2) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
         const unsigned j = perm[k];
         pos2[k] = pos[j];
         if (plo) plo2[k] = plo[j];
         vel2[k] = vel[j];
+        if (vlo) vlo2[k] = vlo[j];
         acc2[k] = acc[j];
         id2[k] = id[j];
     }
@@ -578,8 +581,10 @@ void launch_permute(const Particles& P, const unsigned* perm, long long n, bool 
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
-    permute_kernel<<<(unsigned)blocks, 256, 0, s>>>(perm, n, P.pos, split ? P.plo : nullptr, P.vel, P.acc, P.id,
-                                                     P.pos2, split ? P.plo2 : nullptr, P.vel2, P.acc2, P.id2);
+    permute_kernel<<<(unsigned)blocks, 256, 0, s>>>(perm, n, P.pos, split ? P.plo : nullptr, P.vel,
+                                                     split ? P.vlo : nullptr, P.acc, P.id, P.pos2,
+                                                     split ? P.plo2 : nullptr, P.vel2, split ? P.vlo2 : nullptr,
+                                                     P.acc2, P.id2);
 }
 
 }  // namespace ngrav

@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(kPpThreads) walk_pp_kernel(NodeArrays T, Count
                 hdt_mine = (float)(0.5 * pp.base / (double)(1 << rung));
             }
             const unsigned active = __ballot_sync(0xffffffffu, mine);
+            if (pp.block && lane == 0) atomicAdd(&C->targets, (unsigned long long)__popc(active));
             if (active == 0) continue;
             const float4 tp = mine ? P.pos[slot] : zero;
             const float4 tl = (mine && SPLIT) ? P.plo[slot] : zero;
@@ -231,10 +232,10 @@ __global__ void __launch_bounds__(kPpThreads) walk_pp_kernel(NodeArrays T, Count
                 P.acc[slot] = make_float4(ax, ay, az, 0.f);
                 if (wp.kick) {
                     float4 v = P.vel[slot];
-                    v.x = fmaf(hdt_mine, ax, v.x);
-                    v.y = fmaf(hdt_mine, ay, v.y);
-                    v.z = fmaf(hdt_mine, az, v.z);
+                    float4 vl = SPLIT ? P.vlo[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    kick_v(v, SPLIT ? &vl : nullptr, hdt_mine, make_float4(ax, ay, az, 0.f));
                     P.vel[slot] = v;
+                    if (SPLIT) P.vlo[slot] = vl;
                 }
             }
             if (bad & (kStStackOverflow | kStCorrupt)) break;

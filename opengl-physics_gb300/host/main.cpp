@@ -5,7 +5,7 @@
 //   nbody_gb300 --bench <solver> [--bench-n N] [--bench-theta T] [--bench-reps R] [--bench-eps E]
 //   nbody_gb300 --dump-ic <file.bin> [--bench-n N]
 //   nbody_gb300 --deck <f.toml> --dump-ic <file.bin>   (the deck's scenario; no GPU)
-//   nbody_gb300 --selftest
+//   nbody_gb300 --selftest | --rung-selftest | --dt-selftest
 //   nbody_gb300 --print-deck <f.toml>        (parsed deck as JSON; no GPU)
 // Flags as in main.cpp:35-95; --bench prints the same CSV line
 // (main.cpp:389-391), --dump-ic writes the same raw float32 records
@@ -17,6 +17,7 @@
 #include "scenarios.hpp"
 #include "simulation.hpp"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -31,7 +32,7 @@ namespace {
 struct Args {
     std::string deck, out, bench, dumpIc, printDeck;
     int frames = 0, substeps = 0;
-    bool selftest = false;
+    bool selftest = false, rungSelftest = false, dtSelftest = false;
     int benchN = 10000;
     double benchTheta = 0.5;
     int benchReps = 5;
@@ -50,6 +51,8 @@ Args ParseArgs(int argc, char** argv) {
         else if (s == "--frames") a.frames = std::atoi(next());
         else if (s == "--substeps") a.substeps = std::atoi(next());
         else if (s == "--selftest") a.selftest = true;
+        else if (s == "--rung-selftest") a.rungSelftest = true;
+        else if (s == "--dt-selftest") a.dtSelftest = true;
         else if (s == "--bench") a.bench = next();
         else if (s == "--bench-n") a.benchN = std::atoi(next());
         else if (s == "--bench-theta") a.benchTheta = std::atof(next());
@@ -206,6 +209,180 @@ int SelfTest() {
     return ok ? 0 : 1;
 }
 
+double Energy(ngrav_gpu_ctx* ctx) {
+    ngrav_gpu_diag d;
+    Check(ngrav_gpu_diagnostics(ctx, 1, &d), ctx, "diagnostics");
+    return d.energy;
+}
+
+long long StatsField(ngrav_gpu_ctx* ctx, long long ngrav_gpu_stats::*f) {
+    ngrav_gpu_stats st;
+    Check(ngrav_gpu_get_stats(ctx, &st), ctx, "get_stats");
+    return st.*f;
+}
+
+// CoreRungSelfTest (SelfTest.cpp:821-924) on the GPU path: a 200-body cloud
+// plus a tight binary under the block, global-adaptive and fixed schemes
+// (exact pair sums, theta = 0), and a Barnes-Hut cold collapse under the
+// block scheme.
+int RungSelfTest() {
+    bool ok = true;
+    std::printf("[block / rung timesteps, GPU]\n");
+    {
+        ngrav_host::State cloud = ngrav_host::Plummer(200, 12);
+        ngrav_host::State s;
+        const int n = 202;
+        s.x.assign(n, 0.0); s.y.assign(n, 0.0); s.z.assign(n, 0.0);
+        s.vx.assign(n, 0.0); s.vy.assign(n, 0.0); s.vz.assign(n, 0.0); s.m.assign(n, 0.0);
+        for (int i = 0; i < 200; ++i) {
+            s.x[i] = cloud.x[i] - 8.0;
+            s.y[i] = cloud.y[i];
+            s.z[i] = cloud.z[i];
+            s.vx[i] = cloud.vx[i];
+            s.vy[i] = cloud.vy[i];
+            s.vz[i] = cloud.vz[i];
+            s.m[i] = cloud.m[i];
+        }
+        const double vt = 0.5 * std::sqrt(1.0 * 2.0 / 0.08);
+        s.x[200] = 7.96;
+        s.x[201] = 8.04;
+        s.vy[200] = -vt;
+        s.vy[201] = vt;
+        s.m[200] = s.m[201] = 1.0;
+        const double T = 2.0, dt = 5e-3, eta = 0.02;
+        auto run = [&](int scheme, long long& pevals, double& drift, double& elapsed) {  // 0 block, 1 adaptive, 2 fixed
+            ngrav_gpu_ctx* ctx = MakeContext(1.0, 0.01, 0.0, 8);
+            Check(ngrav_gpu_set_particles(ctx, n, s.x.data(), s.y.data(), s.z.data(), s.vx.data(), s.vy.data(),
+                                          s.vz.data(), s.m.data()),
+                  ctx, "set_particles");
+            Check(ngrav_gpu_prime(ctx), ctx, "prime");
+            const double e0 = Energy(ctx);
+            Check(ngrav_gpu_reset_cumulative(ctx), ctx, "reset_cumulative");
+            double t = 0.0;
+            while (t < T) {
+                if (scheme == 0) {
+                    int rmax = 0;
+                    Check(ngrav_gpu_block_step(ctx, dt, eta, 8, &rmax), ctx, "block_step");
+                    t += dt;
+                } else if (scheme == 1) {
+                    double h = dt;
+                    Check(ngrav_gpu_adaptive_dt(ctx, eta, dt, &h), ctx, "adaptive_dt");
+                    Check(ngrav_gpu_step(ctx, 1, h), ctx, "step");
+                    t += h;
+                } else {
+                    Check(ngrav_gpu_step(ctx, 1, dt), ctx, "step");
+                    t += dt;
+                }
+            }
+            pevals = StatsField(ctx, &ngrav_gpu_stats::cum_particle_evals);
+            elapsed = t;
+            drift = std::abs((Energy(ctx) - e0) / e0);
+            ngrav_gpu_destroy(ctx);
+        };
+        long long pe[3];
+        double dr[3], el[3];
+        for (int k = 0; k < 3; ++k) run(k, pe[k], dr[k], el[k]);
+        const double ratio = pe[0] > 0 ? double(pe[1]) / double(pe[0]) : 0.0;
+        std::printf("  200-body cloud + 1 tight binary, integrated to t=%.1f:\n", T);
+        std::printf("    fixed global    drift %.2e   %lld pevals  (t=%.2f)\n", dr[2], pe[2], el[2]);
+        std::printf("    adaptive global drift %.2e   %lld pevals  (t=%.2f)\n", dr[1], pe[1], el[1]);
+        std::printf("    block           drift %.2e   %lld pevals  (t=%.2f)   (%.1fx fewer than adaptive)\n", dr[0],
+                    pe[0], el[0], ratio);
+        CheckPrint(ok, "block-scheme energy drift", dr[0], 1e-2);
+        CheckPrint(ok, "block uses >=2x fewer force evals than adaptive", ratio >= 2.0 ? 0.0 : 1.0, 0.0);
+    }
+    {
+        ngrav_host::State s = ngrav_host::Plummer(1200, 4);
+        std::fill(s.vx.begin(), s.vx.end(), 0.0);
+        std::fill(s.vy.begin(), s.vy.end(), 0.0);
+        std::fill(s.vz.begin(), s.vz.end(), 0.0);
+        ngrav_gpu_ctx* ctx = MakeContext(1.0, 0.02, 0.5, 8);
+        Check(ngrav_gpu_set_particles(ctx, (int64_t)s.Count(), s.x.data(), s.y.data(), s.z.data(), s.vx.data(),
+                                      s.vy.data(), s.vz.data(), s.m.data()),
+              ctx, "set_particles");
+        Check(ngrav_gpu_prime(ctx), ctx, "prime");
+        const double e0 = Energy(ctx);
+        for (int i = 0; i < 150; ++i) {
+            int rmax = 0;
+            Check(ngrav_gpu_block_step(ctx, 3e-3, 0.03, 5, &rmax), ctx, "block_step");
+        }
+        const double drift = std::abs((Energy(ctx) - e0) / e0);
+        ngrav_gpu_destroy(ctx);
+        std::printf("  BH cold collapse N=1200, 150 base steps: block-scheme energy drift %.2e\n", drift);
+        CheckPrint(ok, "block-scheme BH cold-collapse energy drift", drift, 0.05);
+    }
+    std::printf("\nrung-selftest: %s\n", ok ? "PASS" : "FAIL");
+    return ok ? 0 : 1;
+}
+
+struct KeplerRun {
+    double drift;
+    long long evals;
+};
+
+// RunEccentric (SelfTest.cpp:391-434): an equal-mass pair on an orbit of
+// eccentricity e for `periods` periods, exact pair sum, eps 1e-4; energy
+// sampled every 32 steps; drift = (Emax - Emin) / |mean|.
+KeplerRun RunEccentric(double e, double dt, bool adaptive, double eta, int periods) {
+    const double G = 1.0, m = 1.0, r0 = 1.0;
+    const double a = r0 / (1.0 + e);
+    const double vRel = std::sqrt(G * 2.0 * m * (2.0 / r0 - 1.0 / a));
+    const double period = 2.0 * M_PI * std::sqrt(a * a * a / (G * 2.0 * m));
+    const double x[2] = {-r0 / 2, r0 / 2}, y[2] = {0, 0}, z[2] = {0, 0};
+    const double vx[2] = {0, 0}, vy[2] = {-vRel / 2, vRel / 2}, vz[2] = {0, 0}, mm[2] = {m, m};
+    ngrav_gpu_ctx* ctx = MakeContext(G, 1e-4, 0.0, 8);
+    Check(ngrav_gpu_set_particles(ctx, 2, x, y, z, vx, vy, vz, mm), ctx, "set_particles");
+    Check(ngrav_gpu_prime(ctx), ctx, "prime");
+    const long long ev0 = StatsField(ctx, &ngrav_gpu_stats::force_evals);
+    const double E0 = Energy(ctx);
+    double Emin = E0, Emax = E0, t = 0.0;
+    const double tEnd = periods * period;
+    long long k = 0;
+    while (t < tEnd && k < 20000000) {
+        double h = dt;
+        if (adaptive) Check(ngrav_gpu_adaptive_dt(ctx, eta, dt, &h), ctx, "adaptive_dt");
+        Check(ngrav_gpu_step(ctx, 1, h), ctx, "step");
+        t += h;
+        if ((k++ % 32) == 0) {
+            const double E = Energy(ctx);
+            Emin = std::min(Emin, E);
+            Emax = std::max(Emax, E);
+        }
+    }
+    KeplerRun r;
+    r.drift = (Emax - Emin) / std::abs(0.5 * (Emax + Emin));
+    r.evals = StatsField(ctx, &ngrav_gpu_stats::force_evals) - ev0;
+    ngrav_gpu_destroy(ctx);
+    return r;
+}
+
+// CoreDtSelfTest (SelfTest.cpp:438-482) on the GPU path.
+int DtSelfTest() {
+    bool ok = true;
+    std::printf("[adaptive global dt, GPU]\n");
+    const KeplerRun mild = RunEccentric(0.36, 2.0 * M_PI * std::sqrt(std::pow(1.0 / 1.36, 3) / 2.0) / 2000.0, false,
+                                        0.0, 4);
+    CheckPrint(ok, "fixed-dt mild-orbit energy drift", mild.drift, 1e-4);
+    const double aEcc = 1.0 / 1.9;
+    const double Tecc = 2.0 * M_PI * std::sqrt(aEcc * aEcc * aEcc / 2.0);
+    const KeplerRun ad = RunEccentric(0.9, Tecc / 600.0, true, 0.015, 3);
+    std::printf("  adaptive(eta=0.015): drift=%.3e  evals=%lld\n", ad.drift, ad.evals);
+    CheckPrint(ok, "adaptive e=0.9 energy drift", ad.drift, 1e-3);
+    const KeplerRun c1 = RunEccentric(0.9, Tecc / 4800.0, false, 0.0, 3);
+    const KeplerRun c2 = RunEccentric(0.9, Tecc / 9600.0, false, 0.0, 3);
+    const double p = std::log(c1.drift / c2.drift) / std::log(2.0);
+    const double div = 9600.0 * std::pow(c2.drift / ad.drift, 1.0 / p);
+    const KeplerRun fm = RunEccentric(0.9, Tecc / div, false, 0.0, 3);
+    std::printf("  fixed dt calibration: order p=%.2f, extrapolated div=%.0f -> verified drift=%.3e  evals=%lld\n", p,
+                div, fm.drift, fm.evals);
+    const double ratio = double(fm.evals) / double(std::max(1LL, ad.evals));
+    std::printf("  fixed/adaptive force-eval ratio at matched accuracy = %.2f\n", ratio);
+    CheckPrint(ok, "extrapolation sanity: verified drift within 50% of target", fm.drift / ad.drift - 1.0, 0.5);
+    CheckPrint(ok, "adaptive uses >=2x fewer evals at matched accuracy", std::max(0.0, 2.0 - ratio), 0.0);
+    std::printf("\ndt-selftest: %s\n", ok ? "PASS" : "FAIL");
+    return ok ? 0 : 1;
+}
+
 void PrintValue(const fw::TomlValue& v) {
     switch (v.kind) {
         case fw::TomlValue::Table: {
@@ -265,6 +442,8 @@ int main(int argc, char** argv) {
             return 0;
         }
         if (a.selftest) return SelfTest();
+        if (a.rungSelftest) return RungSelfTest();
+        if (a.dtSelftest) return DtSelfTest();
         if (!a.dumpIc.empty()) return a.deck.empty() ? DumpIc(a) : DumpDeckIc(a);
         if (!a.bench.empty()) return RunBench(a);
         if (a.deck.empty() || a.out.empty()) {
@@ -273,7 +452,7 @@ int main(int argc, char** argv) {
                          "  nbody_gb300 --deck <f.toml> --out <dir> [--frames N] [--substeps N]\n"
                          "  nbody_gb300 --bench <solver> --bench-n N [--bench-theta T] [--bench-reps R]\n"
                          "  nbody_gb300 --dump-ic <file.bin> --bench-n N   (raw f32 x,y,z,m,vx,vy,vz)\n"
-                         "  nbody_gb300 --selftest | --print-deck <f.toml>\n");
+                         "  nbody_gb300 --selftest | --rung-selftest | --dt-selftest | --print-deck <f.toml>\n");
             return 2;
         }
         const fw::Deck deck = fw::Deck::FromFile(a.deck);

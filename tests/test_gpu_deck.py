@@ -9,7 +9,8 @@ and --selftest, all through the C-ABI library.
 - --bench prints the reference's CSV line (main.cpp:389-391) with a mean
   relative force error that is the Barnes-Hut truncation error, not an FP32
   artefact.
-- --selftest runs the Barnes-Hut gates of SelfTest.cpp on the GPU.
+- --selftest, --rung-selftest and --dt-selftest run the gates of
+  SelfTest.cpp (Barnes-Hut, block timesteps, adaptive dt) on the GPU.
 """
 import csv
 import json
@@ -96,6 +97,21 @@ def test_bench_csv_line(exe):
 def test_selftest_passes(exe):
     r = run(exe, "--selftest")
     assert "selftest: PASS" in r.stdout
+
+
+def test_rung_selftest_passes(exe):
+    """CoreRungSelfTest's gates (SelfTest.cpp:821-924) through the C-ABI: the
+    block scheme conserves energy and needs >= 2x fewer particle evaluations
+    than the global-adaptive scheme on a cloud with one tight binary."""
+    r = run(exe, "--rung-selftest")
+    assert "rung-selftest: PASS" in r.stdout, r.stdout
+
+
+def test_dt_selftest_passes(exe):
+    """CoreDtSelfTest's gates (SelfTest.cpp:438-482): adaptive dt on an e = 0.9
+    orbit matches a fixed dt's accuracy with >= 2x fewer evaluations."""
+    r = run(exe, "--dt-selftest")
+    assert "dt-selftest: PASS" in r.stdout, r.stdout
 
 
 def ic_deck(tmp_path, ic, n, seed, body, binary=False):
