@@ -27,6 +27,9 @@ e2e     = the same metric through the C-ABI with host buffers: per step
 roofline: the evaluation kernel (P2P + P2C, FP32 pipe): algorithmic
           flops (20 per P2P pair + 60 per P2C term, device-counted) / its
           event-timed duration, against the measured FP32 FMA peak.
+roofline_sort: the HBM-bound part of the tree build (radix sort + the
+          permutation into key order), algorithmic bytes / event time of
+          that phase, against the measured copy bandwidth.
 cpu_baseline: the oracle (C restatement of the reference's CPU path) on the
           host cores, bounded sample: full tree build + walk over every
           k-th leaf group, extrapolated to a full step.
@@ -93,7 +96,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self._proc = None
             return
@@ -260,6 +263,30 @@ def timed(sim, steps, warmup, dt, clocks=None):
     return st, st["cum_ms_step"] / steps, clk
 
 
+def hbm_peak():
+    """Measured copy bandwidth of the GB300s (driver-written), else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def sort_roofline(st, n, split):
+    """The HBM-bound part of the tree build: the LSD radix sort (8 passes of
+    8-bit digits; each reads and writes 8 B keys + 4 B slots) and the
+    permutation of the state into key order (split: pos, plo, vel, vlo, acc
+    read and written, id moved, the permutation read), algorithmic bytes over
+    the phase's event time."""
+    per = 8 * 24 + ((5 * 16 + 4 + 4) + (5 * 16 + 4) if split else (3 * 16 + 4 + 4) + (3 * 16 + 4))
+    ms = st["ms_sort"]
+    peak, src = hbm_peak()
+    ach = per * n / (ms * 1e-3) / 1e9 if ms > 0 else None
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
+            "traffic": None, "bytes_per_particle": per, "kernel": "radix sort (rs_hist, rs_scatter) + permute",
+            "peak_source": src}
+
+
 def phases(st):
     return {k: st[k] for k in ("ms_bbox_keys", "ms_sort", "ms_build", "ms_moments", "ms_walk", "ms_force")}
 
@@ -267,7 +294,7 @@ def phases(st):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="galaxy4m", choices=sorted(WORKLOADS))
@@ -485,6 +512,7 @@ def main():
                          "traffic_unit": "DRAM bytes per eval_kernel launch (ncu bytes/entry x entries)",
                          "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
                          "peak_source": "measured FP32 FMA probe (ngrav_gpu_probe_fp32_peak)"},
+            "roofline_sort": sort_roofline(st, n, args.precision == "split"),
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,
         }
         print(json.dumps(line), flush=True)
