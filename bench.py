@@ -252,14 +252,37 @@ def calibrate(sim, grid, setter, target=TARGET_RMS):
     return (best if best is not None else grid[0]), table
 
 
-def timed(sim, steps, warmup, dt, clocks=None):
+def replica_max(v, dist, device):
+    """The largest of a per-rank figure over the replicas (the slowest one sets
+    the pace of the job); v itself with one process."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(n, world, ms_max):
+    """Whole-job particle-steps/s: every replica advances n particles per step."""
+    return world * n / (ms_max * 1e-3)
+
+
+def timed(sim, steps, warmup, dt, clocks=None, dist=None):
+    """W untimed steps, then exactly K steps between barriers (each
+    ngrav_gpu_step call returns with its stream synchronised); the time is the
+    device time of the K steps on the engine's stream."""
     sim.step(warmup, dt)
+    if dist is not None:
+        dist.barrier()
     if clocks:
         clocks.start()
     sim.reset_cumulative()
     sim.step(steps, dt)
     st = sim.stats()
     clk = clocks.stop() if clocks else None
+    if dist is not None:
+        dist.barrier()
     return st, st["cum_ms_step"] / steps, clk
 
 
@@ -398,9 +421,10 @@ def main():
     # ---- geometric (plain theta) arm ----
     restart(ncrit_t)
     sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
-    st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks)
+    st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks, dist)
+    ms_g = replica_max(ms_g, dist, f"cuda:{dev}")
     fe_g = error_at(sim)
-    arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "value": world * n / (ms_g * 1e-3), "ms_per_step": ms_g,
+    arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "value": job_value(n, world, ms_g), "ms_per_step": ms_g,
                  "force_err_rms": fe_g["rms"], "force_err_max": fe_g["max"],
                  "p2p_pairs_per_step": st_g["cum_p2p_pairs"] / max(1, st_g["cum_evals"]),
                  "p2c_terms_per_step": st_g["cum_p2c_terms"] / max(1, st_g["cum_evals"]),
@@ -415,17 +439,12 @@ def main():
         sim.set_opts(theta=best_l["theta"], mac=pkg.MAC_LEARNED)
         sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=TARGET_RMS * 1.5)
         sim.lmac_reset()
-        st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks)
+        st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks, dist)
         fe = error_at(sim)
     else:
         st, ms_step, clk, fe = st_g, ms_g, clk_g, fe_g
-    ms_max = ms_step
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms_step], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * n / (ms_max * 1e-3)
+    ms_max = replica_max(ms_step, dist, f"cuda:{dev}")
+    value = job_value(n, world, ms_max)
 
     # roofline of the evaluation kernel (P2P + P2C on the FP32 pipe)
     flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
@@ -462,7 +481,8 @@ def main():
         for a, b in zip(hin, hout):
             a[:] = b  # the next step starts from this step's result
     e2e_ms = 1e3 * float(np.mean(t_e2e))
-    e2e = {"value": world * n / (e2e_ms * 1e-3), "unit": "particle-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
+    e2e_ms = replica_max(e2e_ms, dist, f"cuda:{dev}")
+    e2e = {"value": job_value(n, world, e2e_ms), "unit": "particle-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
            "d2h_bytes_per_step": 6 * 8 * n, "ms_per_step": e2e_ms,
            "call": "ngrav_gpu_set_state_f32 + ngrav_gpu_step(1) + ngrav_gpu_get_state (pinned host buffers)"}
 
