@@ -402,13 +402,25 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
         const int fc = T.first_child[node];
         if (fc < 0) continue;
         const int nch = T.nchild[node];
+        // the (at most eight) children unrolled: their loads and the FP64
+        // chains of the combination overlap instead of running one child
+        // after another
+        double mc[8], cxs[8], cys[8], czs[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const bool in = k < nch;
+            mc[k] = in ? T.mass[fc + k] : 0.0;
+            cxs[k] = in ? T.comx[fc + k] : 0.0;
+            cys[k] = in ? T.comy[fc + k] : 0.0;
+            czs[k] = in ? T.comz[fc + k] : 0.0;
+        }
         double PM = 0.0, px = 0.0, py = 0.0, pz = 0.0;
-        for (int c = fc; c < fc + nch; ++c) {
-            const double mc = T.mass[c];
-            PM += mc;
-            px = fma(mc, T.comx[c], px);
-            py = fma(mc, T.comy[c], py);
-            pz = fma(mc, T.comz[c], pz);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {  // in child order, as the sequential sum
+            PM += mc[k];
+            px = fma(mc[k], cxs[k], px);
+            py = fma(mc[k], cys[k], py);
+            pz = fma(mc[k], czs[k], pz);
         }
         double pcx = T.cx[node], pcy = T.cy[node], pcz = T.cz[node];
         if (PM > 0.0) {
@@ -418,25 +430,21 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
             pcz = pz * inv;
         }
         double PQ[5] = {0, 0, 0, 0, 0};
-        if (quadrupole) {
-            for (int c = fc; c < fc + nch; ++c) {
-                const double mc = T.mass[c];
-                if (mc <= 0.0) continue;
-                const double dx = T.comx[c] - pcx, dy = T.comy[c] - pcy, dz = T.comz[c] - pcz;
-                const double d2 = dx * dx + dy * dy + dz * dz;
-                PQ[0] += T.quad[5 * c + 0] + mc * (3.0 * dx * dx - d2);
-                PQ[1] += T.quad[5 * c + 1] + mc * (3.0 * dy * dy - d2);
-                PQ[2] += T.quad[5 * c + 2] + mc * 3.0 * dx * dy;
-                PQ[3] += T.quad[5 * c + 3] + mc * 3.0 * dx * dz;
-                PQ[4] += T.quad[5 * c + 4] + mc * 3.0 * dy * dz;
-            }
-        }
         double mr = 0.0;
-        if (PM > 0.0) {
-            for (int c = fc; c < fc + nch; ++c) {
-                const double dx = T.comx[c] - pcx, dy = T.comy[c] - pcy, dz = T.comz[c] - pcz;
-                mr = fmax(mr, T.maxr[c] + sqrt(dx * dx + dy * dy + dz * dz));
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (k >= nch) break;
+            const int c = fc + k;
+            const double dx = cxs[k] - pcx, dy = cys[k] - pcy, dz = czs[k] - pcz;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (quadrupole && mc[k] > 0.0) {
+                PQ[0] += T.quad[5 * c + 0] + mc[k] * (3.0 * dx * dx - d2);
+                PQ[1] += T.quad[5 * c + 1] + mc[k] * (3.0 * dy * dy - d2);
+                PQ[2] += T.quad[5 * c + 2] + mc[k] * 3.0 * dx * dy;
+                PQ[3] += T.quad[5 * c + 3] + mc[k] * 3.0 * dx * dz;
+                PQ[4] += T.quad[5 * c + 4] + mc[k] * 3.0 * dy * dz;
             }
+            if (PM > 0.0) mr = fmax(mr, T.maxr[c] + sqrt(d2));
         }
         T.mass[node] = PM;
         T.comx[node] = pcx;
