@@ -328,7 +328,7 @@ def main():
     ap.add_argument("--lmac-pairs", type=int, default=1 << 22)
     ap.add_argument("--lmac-snapshots", type=int, default=16)
     ap.add_argument("--precision", default="split", choices=["split", "plain"])
-    ap.add_argument("--leaf-grid", default="16,24,32,48",
+    ap.add_argument("--leaf-grid", default="16,24,32,40,48",
                     help="leaf capacities tried per arm (comma list; one value fixes it)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
