@@ -17,10 +17,11 @@
 // per leaf, completing on an mbarrier with a bounded wait) into a 4 KiB
 // shared-memory buffer, each batch as many leaves (up to 32) as fit by
 // their actual counts; the next batch's leaf records load while a batch is
-// in flight.  (A second
-// buffer would overlap copy and compute within the warp, but halves the
-// resident warps; measured slower.)  In SPLIT precision each lane's partial
-// sums are Kahan compensated once per staged chunk.
+// in flight.  (A second buffer would overlap copy and compute within the
+// warp, but halves the resident warps; measured slower.)  In SPLIT precision
+// the staged sources then move from their leaves' frames into the group's,
+// one lane per source, and each lane's partial sums are Kahan compensated
+// once per staged chunk.
 #include "engine.cuh"
 #include "softening.cuh"
 
@@ -40,7 +41,6 @@ struct __align__(128) EvalSmem {
     float red[3][32];                         // slice reduction
     float4 shift[kBuffers][32];               // near-leaf frame shift (SPLIT)
     int start[kBuffers][32];
-    int cnt[kBuffers][32];
     int pre[kBuffers][33];
     unsigned long long bar[2];
 };
@@ -249,7 +249,6 @@ __device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& 
     int tot;
     const int ex = excl_scan(in.cnt, lane, tot);
     sm.start[b][lane] = in.start;
-    sm.cnt[b][lane] = in.cnt;
     sm.pre[b][lane] = ex;
     if (lane == 31) sm.pre[b][32] = tot;
     sm.shift[b][lane] = in.shift;
@@ -290,6 +289,32 @@ __device__ __forceinline__ int stage_fitting(EvalSmem& sm, const NearInfo& in, i
     NearInfo mine = in;
     if (lane >= nb) mine.cnt = 0;
     return stage_batch(sm, 0, mine, lane, src);
+}
+
+// Moves a staged batch of ns sources from their leaves' frames into the
+// group's frame, lane-parallel over sources (lane = slot within a window of
+// 32).  Source j belongs to the last of the nb staged leaves whose first
+// slot is <= j; leaves hold at least one source, so their first slots are
+// distinct and bit i of a window's mask marks a leaf starting at slot
+// base + i.  (Lanes past the near list stage nothing and start at slot ns.)
+__device__ __forceinline__ void shift_batch(EvalSmem& sm, int ns, int nb, int lane) {
+    const int first = lane < nb ? sm.pre[0][lane] : ns;
+    int before = 0;  // leaves starting before the window
+    for (int base = 0; base < ns; base += 32) {
+        const unsigned bit = first >= base && first < base + 32 ? 1u << (first - base) : 0u;
+        const unsigned starts = __reduce_or_sync(0xffffffffu, bit);
+        const int j = base + lane;
+        if (j < ns) {
+            const int leaf = before + __popc(starts & (0xffffffffu >> (31 - lane))) - 1;
+            const float4 sh = sm.shift[0][leaf];
+            float4 v = sm.src[0][j];
+            v.x += sh.x;
+            v.y += sh.y;
+            v.z += sh.z;
+            sm.src[0][j] = v;
+        }
+        before += __popc(starts);
+    }
 }
 
 template <bool SPLIT, bool QUAD, int SOFT>
@@ -407,17 +432,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                         break;
                     }
                     phase[0] ^= 1u;
-                    if (SPLIT && lane < nb_cur) {  // move staged sources into the group's frame
-                        const float4 sh = sm.shift[0][lane];
-                        float4* q = &sm.src[0][sm.pre[0][lane]];
-                        for (int kk = 0; kk < sm.cnt[0][lane]; ++kk) {
-                            float4 v = q[kk];
-                            v.x += sh.x;
-                            v.y += sh.y;
-                            v.z += sh.z;
-                            q[kk] = v;
-                        }
-                    }
+                    if (SPLIT) shift_batch(sm, ns_cur, nb_cur, lane);  // into the group's frame
                     __syncwarp();
                     p2p_chunk<SPLIT, SOFT>(g, sm.src[0], ns_cur, wp.eps2, wp.ih);
                     __syncwarp();
