@@ -11,7 +11,11 @@
 //
 // GB300 mapping.  One warp per group (dynamic scheduling), lane = (target t,
 // slice s): nt targets x floor(32/nt) source slices, slices summed at the end
-// of the group.  Far records are staged 32 at a time into shared memory in
+// of the group.  A group's targets run in blocks of up to 64, each in one or
+// two passes over every staged chunk (split to keep the lanes busy: 20
+// targets as 4 x 8 + 16 x 2 slices), the second pass's sums parked in shared
+// memory; 72 registers and 7.6 KiB of shared memory per warp keep 7 CTAs of
+// 4 warps per SM.  Far records are staged 32 at a time into shared memory in
 // the group's frame, the next batch loading into registers while this one is
 // evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
 // per leaf, completing on an mbarrier with a bounded wait) into a 4 KiB
@@ -39,6 +43,9 @@ struct __align__(128) EvalSmem {
     float4 farB[32];                          //   Qxx Qyy Qxy Qxz
     float farQ[32];                           //   Qyz
     float red[3][32];                         // slice reduction
+    float4 pass_tgt[32];                      // second pass of a target block: target, packed lane map
+    float4 pass_acc[32];                      //   running sums ax ay az, compensation cx
+    float2 pass_cmp[32];                      //   compensation cy cz
     float4 shift[kBuffers][32];               // near-leaf frame shift (SPLIT)
     int start[kBuffers][32];
     int pre[kBuffers][33];
@@ -124,6 +131,94 @@ __device__ __forceinline__ void accumulate(Lane& g, float px, float py, float pz
         g.ax += px;
         g.ay += py;
         g.az += pz;
+    }
+}
+
+// Target blocks of up to 64 targets run in one or two passes over each
+// staged chunk: pass 0 takes the first `first[n]` targets, pass 1 the rest,
+// each with floor(32 / targets) source slices.  The split minimises the
+// source steps per staged source, 1/S0 + 1/S1 (plus 0.03 per extra pass for
+// its loop and accumulator traffic), against one pass of all n (1/S, n <= 32):
+// a block of 20 targets runs as 4 x 8 slices + 16 x 2 slices (0.625 steps
+// per source) instead of 20 lanes with 12 idle (1 step), and a block of 40
+// as 8 x 4 + 32 x 1 without staging its lists twice.
+constexpr int kBlockTargets = 64;
+struct PassSplit {
+    unsigned char first[kBlockTargets + 1];
+};
+constexpr PassSplit make_pass_split() {
+    PassSplit t{};
+    for (int n = 1; n <= kBlockTargets; ++n) {
+        float best = n <= 32 ? 1.f / (float)(32 / n) : 1e30f;
+        int b0 = n <= 32 ? n : 32;
+        for (int a = 1; a < n && a <= 32; ++a) {
+            const int b = n - a;
+            if (b > 32) continue;
+            const float c = 1.f / (float)(32 / a) + 1.f / (float)(32 / b) + 0.03f;
+            if (c < best) {
+                best = c;
+                b0 = a;
+            }
+        }
+        t.first[n] = (unsigned char)b0;
+    }
+    return t;
+}
+__constant__ PassSplit kPassSplit = make_pass_split();
+
+// Lane map of nt <= 32 targets starting at slot `first`, sums zeroed.
+__device__ __forceinline__ Lane make_lane(const float4* __restrict__ src, int first, int nt, int lane) {
+    Lane g;
+    g.nt = nt;
+    g.S = 32 / nt;
+    g.active = lane < nt * g.S;
+    g.sl = lane / nt;
+    const float4 tp = src[first + lane % nt];
+    g.tx = tp.x;
+    g.ty = tp.y;
+    g.tz = tp.z;
+    g.ax = g.ay = g.az = g.cx = g.cy = g.cz = 0.f;
+    return g;
+}
+
+__device__ __forceinline__ void save_pass(EvalSmem& sm, const Lane& g, int lane) {
+    const int map = g.sl | (g.S << 8) | (g.nt << 16) | ((int)g.active << 24);
+    sm.pass_tgt[lane] = make_float4(g.tx, g.ty, g.tz, __int_as_float(map));
+    sm.pass_acc[lane] = make_float4(g.ax, g.ay, g.az, g.cx);
+    sm.pass_cmp[lane] = make_float2(g.cy, g.cz);
+}
+
+__device__ __forceinline__ Lane load_pass(const EvalSmem& sm, int lane) {
+    Lane g;
+    const float4 t = sm.pass_tgt[lane], a = sm.pass_acc[lane];
+    const float2 c = sm.pass_cmp[lane];
+    const int map = __float_as_int(t.w);
+    g.tx = t.x;
+    g.ty = t.y;
+    g.tz = t.z;
+    g.sl = map & 0xFF;
+    g.S = (map >> 8) & 0xFF;
+    g.nt = (map >> 16) & 0xFF;
+    g.active = (map >> 24) != 0;
+    g.ax = a.x;
+    g.ay = a.y;
+    g.az = a.z;
+    g.cx = a.w;
+    g.cy = c.x;
+    g.cz = c.y;
+    return g;
+}
+
+// Applies `f` (one chunk's evaluation) to pass 0 (registers) and, for a
+// two-pass block, to pass 1 (shared memory).
+template <class F>
+__device__ __forceinline__ void for_passes(Lane& g, bool two, EvalSmem& sm, int lane, F&& f) {
+    f(g);
+    if (two) {
+        Lane h = load_pass(sm, lane);
+        f(h);
+        sm.pass_acc[lane] = make_float4(h.ax, h.ay, h.az, h.cx);
+        sm.pass_cmp[lane] = make_float2(h.cy, h.cz);
     }
 }
 
@@ -317,8 +412,41 @@ __device__ __forceinline__ void shift_batch(EvalSmem& sm, int ns, int nb, int la
     }
 }
 
+// Sums the slices of each of a pass's targets (slots first .. first+nt-1),
+// writes the accelerations and applies the closing half kick.
+template <bool SPLIT>
+__device__ __forceinline__ void finish_targets(EvalSmem& sm, const Lane& g, int first, int lane,
+                                               const WalkParams& wp, float4* __restrict__ acc,
+                                               float4* __restrict__ vel, float4* __restrict__ vlo) {
+    if (g.active) {
+        sm.red[0][lane] = g.ax;
+        sm.red[1][lane] = g.ay;
+        sm.red[2][lane] = g.az;
+    }
+    __syncwarp();
+    if (lane < g.nt) {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int s = 0; s < g.S; ++s) {
+            sx += sm.red[0][lane + s * g.nt];
+            sy += sm.red[1][lane + s * g.nt];
+            sz += sm.red[2][lane + s * g.nt];
+        }
+        const float ax = wp.G * sx, ay = wp.G * sy, az = wp.G * sz;
+        const int slot = first + lane;
+        acc[slot] = make_float4(ax, ay, az, 0.f);
+        if (wp.kick) {
+            float4 v = vel[slot];
+            float4 vl = SPLIT ? vlo[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+            kick_v(v, SPLIT ? &vl : nullptr, wp.hdt, make_float4(ax, ay, az, 0.f));
+            vel[slot] = v;
+            if (SPLIT) vlo[slot] = vl;
+        }
+    }
+    __syncwarp();
+}
+
 template <bool SPLIT, bool QUAD, int SOFT>
-__global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counters* C,
+__global__ void __launch_bounds__(kEvalThreads, 7) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
                                                             float4* __restrict__ acc, float4* __restrict__ vel,
                                                             float4* __restrict__ vlo,
@@ -358,17 +486,12 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
             gchi = T.chi[leaf];
             gclo = T.clo[leaf];
         }
-        for (int t0 = 0; t0 < gcount; t0 += 32) {
-            Lane g;
-            g.nt = min(32, gcount - t0);
-            g.S = 32 / g.nt;
-            g.active = lane < g.nt * g.S;
-            g.sl = lane / g.nt;
-            const float4 tp = src[gstart + t0 + lane % g.nt];
-            g.tx = tp.x;
-            g.ty = tp.y;
-            g.tz = tp.z;
-            g.ax = g.ay = g.az = g.cx = g.cy = g.cz = 0.f;
+        for (int t0 = 0; t0 < gcount; t0 += kBlockTargets) {
+            const int nblk = min(kBlockTargets, gcount - t0);
+            const int b0 = kPassSplit.first[nblk];
+            const bool two = b0 < nblk;
+            Lane g = make_lane(src, gstart + t0, b0, lane);
+            if (two) save_pass(sm, make_lane(src, gstart + t0 + b0, nblk - b0, lane), lane);
 
             // ---- far field: batches of 32 records; the next batch loads while this one computes ----
             {
@@ -405,11 +528,14 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                             if (QUAD) B = T.wB[node];
                         }
                     }
-                    p2c_chunk<SPLIT, QUAD, SOFT>(g, sm.farA, sm.farB, sm.farQ, min(32, nfar - b), wp.eps2, wp.ih);
+                    const int nrec = min(32, nfar - b);
+                    for_passes(g, two, sm, lane, [&](Lane& x) {
+                        p2c_chunk<SPLIT, QUAD, SOFT>(x, sm.farA, sm.farB, sm.farQ, nrec, wp.eps2, wp.ih);
+                    });
                     __syncwarp();
                 }
             }
-            p2c += (unsigned long long)g.nt * (unsigned long long)nfar;
+            p2c += (unsigned long long)nblk * (unsigned long long)nfar;
 
             // ---- near field: batches of up to 32 leaves (as many as fit the
             // staging buffer, by their actual counts) staged by TMA ----
@@ -434,7 +560,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                     phase[0] ^= 1u;
                     if (SPLIT) shift_batch(sm, ns_cur, nb_cur, lane);  // into the group's frame
                     __syncwarp();
-                    p2p_chunk<SPLIT, SOFT>(g, sm.src[0], ns_cur, wp.eps2, wp.ih);
+                    for_passes(g, two, sm, lane,
+                               [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src[0], ns_cur, wp.eps2, wp.ih); });
                     __syncwarp();
                     total += ns_cur;
                     // stage the next batch (its info is in registers), then fetch
@@ -481,40 +608,19 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(NodeArrays T, Counte
                             sm.src[0][j] = v;
                         }
                         __syncwarp();
-                        p2p_chunk<SPLIT, SOFT>(g, sm.src[0], ns, wp.eps2, wp.ih);
+                        for_passes(g, two, sm, lane,
+                                   [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src[0], ns, wp.eps2, wp.ih); });
                     }
                     __syncwarp();
                     total += cn;
                 }
             }
             if (timeout) break;
-            pairs += (unsigned long long)g.nt * (unsigned long long)total - (unsigned long long)g.nt;
+            pairs += (unsigned long long)nblk * (unsigned long long)total - (unsigned long long)nblk;
 
             // ---- sum the slices of each target, write a, closing kick ----
-            if (g.active) {
-                sm.red[0][lane] = g.ax;
-                sm.red[1][lane] = g.ay;
-                sm.red[2][lane] = g.az;
-            }
-            __syncwarp();
-            if (lane < g.nt) {
-                float sx = 0.f, sy = 0.f, sz = 0.f;
-                for (int s = 0; s < g.S; ++s) {
-                    sx += sm.red[0][lane + s * g.nt];
-                    sy += sm.red[1][lane + s * g.nt];
-                    sz += sm.red[2][lane + s * g.nt];
-                }
-                const float ax = wp.G * sx, ay = wp.G * sy, az = wp.G * sz;
-                const int slot = gstart + t0 + lane;
-                acc[slot] = make_float4(ax, ay, az, 0.f);
-                if (wp.kick) {
-                    float4 v = vel[slot];
-                    float4 vl = SPLIT ? vlo[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
-                    kick_v(v, SPLIT ? &vl : nullptr, wp.hdt, make_float4(ax, ay, az, 0.f));
-                    vel[slot] = v;
-                    if (SPLIT) vlo[slot] = vl;
-                }
-            }
+            finish_targets<SPLIT>(sm, g, gstart + t0, lane, wp, acc, vel, vlo);
+            if (two) finish_targets<SPLIT>(sm, load_pass(sm, lane), gstart + t0 + b0, lane, wp, acc, vel, vlo);
             __syncwarp();
         }
         if (timeout) break;

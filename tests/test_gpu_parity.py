@@ -134,7 +134,9 @@ def test_determinism_bitwise(pkg, ic):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("n,ncrit", [(131072, 16), (65536, 8)])
+# leaf capacities past 32 run target blocks in two passes (40, 64) and in
+# more than one 64-target block (100)
+@pytest.mark.parametrize("n,ncrit", [(131072, 16), (65536, 8), (65536, 40), (65536, 64), (32768, 100)])
 def test_medium_plummer_vs_oracle(pkg, oracle, ic, n, ncrit):
     x, y, z, vx, vy, vz, m = (a.astype(np.float64) for a in ic.plummer(n, seed=11))
     rx, ry, rz, cnt = oracle.bh_accel(x, y, z, m, 1.0, 0.005, 0.5, ncrit, counters=True)
