@@ -58,6 +58,7 @@ void free_particles(ngrav_gpu_ctx* ctx) {
     P.cap = 0;
     SortBuffers& S = ctx->SB;
     dfree(S.keys); dfree(S.keys_alt); dfree(S.vals); dfree(S.vals_alt); dfree(S.hist); dfree(S.scan_tmp);
+    dfree(S.ktab);
     S.cap = 0;
     dfree(ctx->leaf_at); dfree(ctx->flags); dfree(ctx->scanbuf); dfree(ctx->leaf_list);
     dfree(ctx->stage); dfree(ctx->inv);
@@ -92,6 +93,7 @@ int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
     NG_CUDA(dalloc(S.hist, S.hist_cap));
     S.scan_tmp_cap = scan_tmp_size(std::max(S.hist_cap, c)) + 16;
     NG_CUDA(dalloc(S.scan_tmp, S.scan_tmp_cap));
+    NG_CUDA(dalloc(S.ktab, 3 * (long long)kKeyTabSize));
     S.cap = c;
     NG_CUDA(dalloc(ctx->leaf_at, c)); NG_CUDA(dalloc(ctx->flags, c)); NG_CUDA(dalloc(ctx->scanbuf, c));
     NG_CUDA(dalloc(ctx->leaf_list, c)); NG_CUDA(dalloc(ctx->inv, c));
@@ -208,7 +210,8 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
         launch_forest_root(ctx->F, s);
         ctx->launches += 2;
     }
-    launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->F, ctx->SB.keys, ctx->SB.vals, s);
+    ctx->launches += launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->F, ctx->SB.ktab, ctx->SB.keys,
+                                 ctx->SB.vals, s) - 1;
     rec(ctx, 1);
     const int passes = 8;
     radix_sort_pairs(ctx->SB, n, passes, s);

@@ -22,6 +22,8 @@
 namespace ngrav {
 
 constexpr int kKeyLevels = 21;          // 63-bit keys: 3 bits per level
+constexpr int kKeyTabLevels = 14;       // key levels whose centres are tabulated per build
+constexpr int kKeyTabSize = 1 << kKeyTabLevels;  // table entries per axis (entry 0 unused)
 constexpr int kMaxLevels = kKeyLevels + 1;
 
 // Device status word bits (sticky within one force evaluation).
@@ -157,6 +159,7 @@ struct SortBuffers {
     unsigned* scan_tmp = nullptr;
     long long hist_cap = 0;
     long long scan_tmp_cap = 0;
+    double* ktab = nullptr;           // centres of the top key levels, 3 x kKeyTabSize
 };
 
 struct WalkParams {
@@ -248,8 +251,10 @@ void launch_forest_bbox(const float4* pos, const float4* plo, long long n, const
                         cudaStream_t s);
 void launch_forest_root(const Forest& F, cudaStream_t s);
 void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s);
-void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F,
-                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
+// Keys of the current order (vals = 0 .. n-1); a single system also fills
+// the centre table ktab (3 * kKeyTabSize doubles).  Returns the launches made.
+int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
+                unsigned long long* keys, unsigned* vals, cudaStream_t s);
 // Stable LSD radix sort of (keys, vals) over bits [0, 8*passes); result ends
 // in (keys, vals) (the alternates are scratch).
 void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s);

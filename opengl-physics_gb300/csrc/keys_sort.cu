@@ -239,6 +239,53 @@ __device__ __forceinline__ unsigned axis_bits(double p, double c, double h) {
     return bits;
 }
 
+// The centre recurrence of an axis depends only on that axis's own octant
+// bits, so the centres of levels 0 .. kKeyTabLevels-1 are tabulated once per
+// build: an implicit binary tree per axis, entry 1 the root centre and entry
+// 2e + b the child of entry e on side b (b = 1: p >= c).  Each entry replays
+// exactly the FP64 additions of the walk down to it, so the keys kernel looks
+// the top levels up and adds in FP64 only below them (7 additions per axis
+// instead of 21).
+__global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restrict__ C, double* __restrict__ tab) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * kKeyTabSize) return;
+    const int axis = i / kKeyTabSize, e = i % kKeyTabSize;
+    if (e == 0) return;
+    const int l = 31 - __clz(e);  // level of entry e: its bits below the leading one are levels 0 .. l-1
+    double c = C->root_center[axis];
+    long long hb = __double_as_longlong(C->root_half);
+    for (int k = l - 1; k >= 0; --k) {
+        hb -= 1ll << 52;
+        c = __dadd_rn(c, __longlong_as_double((e >> k) & 1 ? hb : (hb | (long long)0x8000000000000000ull)));
+    }
+    tab[i] = c;
+}
+
+// axis_bits over all kKeyLevels levels with the top kKeyTabLevels looked up
+// in the axis's table.
+__device__ __forceinline__ unsigned axis_bits_tab(double p, const double* __restrict__ tab, double h0) {
+    const long long op = ordered_bits(p);
+    unsigned e = 1;
+#pragma unroll
+    for (int l = 0; l < kKeyTabLevels; ++l) e = 2 * e + (op >= ordered_bits(__ldg(tab + e)) ? 1u : 0u);
+    // continue from the centre of level kKeyTabLevels: the last tabulated
+    // centre plus or minus h / 2^kKeyTabLevels, as the recurrence would
+    long long hb = __double_as_longlong(h0) - ((long long)kKeyTabLevels << 52);
+    double c = __dadd_rn(__ldg(tab + (e >> 1)),
+                         __longlong_as_double(e & 1 ? hb : (hb | (long long)0x8000000000000000ull)));
+    unsigned bits = e - (1u << kKeyTabLevels);
+#pragma unroll
+    for (int l = kKeyTabLevels; l < kKeyLevels; ++l) {
+        const bool b = op >= ordered_bits(c);
+        bits = (bits << 1) | (b ? 1u : 0u);
+        if (l + 1 < kKeyLevels) {
+            hb -= 1ll << 52;
+            c = __dadd_rn(c, __longlong_as_double(b ? hb : (hb | (long long)0x8000000000000000ull)));
+        }
+    }
+    return bits;
+}
+
 // Spread 21 bits so bit k lands at 3k.
 __device__ __forceinline__ unsigned long long spread3(unsigned v) {
     unsigned long long x = v & 0x1FFFFFull;
@@ -252,9 +299,9 @@ __device__ __forceinline__ unsigned long long spread3(unsigned v) {
 
 __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ pos, const float4* __restrict__ plo,
                                                    long long n, const Counters* __restrict__ C,
+                                                   const double* __restrict__ tab,
                                                    unsigned long long* __restrict__ keys,
                                                    unsigned* __restrict__ vals) {
-    const double cx = C->root_center[0], cy = C->root_center[1], cz = C->root_center[2];
     const double h0 = C->root_half;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float4 p = pos[i];
@@ -265,9 +312,9 @@ __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ po
             py += (double)l.y;
             pz += (double)l.z;
         }
-        const unsigned bx = axis_bits<kKeyLevels>(px, cx, h0);
-        const unsigned by = axis_bits<kKeyLevels>(py, cy, h0);
-        const unsigned bz = axis_bits<kKeyLevels>(pz, cz, h0);
+        const unsigned bx = axis_bits_tab(px, tab, h0);
+        const unsigned by = axis_bits_tab(py, tab + kKeyTabSize, h0);
+        const unsigned bz = axis_bits_tab(pz, tab + 2 * kKeyTabSize, h0);
         keys[i] = spread3(bx) | (spread3(by) << 1) | (spread3(bz) << 2);
         vals[i] = (unsigned)i;
     }
@@ -301,14 +348,17 @@ __global__ void __launch_bounds__(256) forest_keys_kernel(const float4* __restri
     }
 }
 
-void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F,
-                 unsigned long long* keys, unsigned* vals, cudaStream_t s) {
+int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
+                unsigned long long* keys, unsigned* vals, cudaStream_t s) {
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
     const unsigned g = (unsigned)blocks;
     switch (F.sys_levels) {
-        case 0: keys_kernel<<<g, 256, 0, s>>>(pos, plo, n, C, keys, vals); break;
+        case 0:
+            key_table_kernel<<<(3 * kKeyTabSize + 255) / 256, 256, 0, s>>>(C, ktab);
+            keys_kernel<<<g, 256, 0, s>>>(pos, plo, n, C, ktab, keys, vals);
+            return 2;
         case 1: forest_keys_kernel<1><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
         case 2: forest_keys_kernel<2><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
         case 3: forest_keys_kernel<3><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
@@ -316,6 +366,7 @@ void launch_keys(const float4* pos, const float4* plo, long long n, Counters* C,
         case 5: forest_keys_kernel<5><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
         default: forest_keys_kernel<6><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
     }
+    return 1;
 }
 
 // ---------------------------------------------------------------------------
