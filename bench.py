@@ -228,8 +228,9 @@ def run_reference(args, rank, world):
     return 0
 
 
-THETA_GRID = (0.5, 0.55, 0.6, 0.625, 0.65, 0.675, 0.7, 0.75, 0.8)
-BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 3e-4, 3.5e-4, 4e-4, 5e-4, 7e-4, 1e-3)
+THETA_GRID = (0.5, 0.55, 0.575, 0.6, 0.6125, 0.625, 0.6375, 0.65, 0.6625, 0.675, 0.7, 0.75, 0.8)
+BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 2.75e-4, 3e-4, 3.25e-4, 3.5e-4, 3.75e-4, 4e-4, 4.5e-4, 5e-4,
+               7e-4, 1e-3)
 TARGET_RMS = 1e-3
 
 
