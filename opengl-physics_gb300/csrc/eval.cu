@@ -41,7 +41,7 @@ struct __align__(128) EvalSmem {
     float4 src[kBuffers][kSrcCap];            // TMA destinations
     float4 farA[32];                          // far batch: COM in the group frame, mass
     float4 farB[32];                          //   Qxx Qyy Qxy Qxz
-    float farQ[32];                           //   Qyz
+    float2 farQ[32];                          //   Qyz, Qzz = -(Qxx + Qyy)
     float red[3][32];                         // slice reduction
     float4 pass_tgt[32];                      // second pass of a target block: target, packed lane map
     float4 pass_acc[32];                      //   running sums ax ay az, compensation cx
@@ -278,7 +278,7 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_
 
 template <bool SPLIT, bool QUAD, int SOFT>
 __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA, const float4* __restrict__ fB,
-                                          const float* __restrict__ fQ, int nf, float eps2, float ih) {
+                                          const float2* __restrict__ fQ, int nf, float eps2, float ih) {
     if (!g.active) return;
     float px = 0.f, py = 0.f, pz = 0.f;
     const float tx = g.tx, ty = g.ty, tz = g.tz;
@@ -287,24 +287,25 @@ __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA
         const float dx = A.x - tx, dy = A.y - ty, dz = A.z - tz;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const float fm = pair_factor<SOFT == 2 ? kSoftSpline : kSoftPlummer>(r2, A.w, eps2, ih);
-        px = fmaf(fm, dx, px);
-        py = fmaf(fm, dy, py);
-        pz = fmaf(fm, dz, pz);
         if (QUAD) {
             const float4 B = fB[f];
-            const float qyz = fQ[f];
-            const float qzz = -(B.x + B.y);
+            const float2 Q = fQ[f];  // Qyz, Qzz
             const float qdx = fmaf(B.x, dx, fmaf(B.z, dy, B.w * dz));
-            const float qdy = fmaf(B.z, dx, fmaf(B.y, dy, qyz * dz));
-            const float qdz = fmaf(B.w, dx, fmaf(qyz, dy, qzz * dz));
+            const float qdy = fmaf(B.z, dx, fmaf(B.y, dy, Q.x * dz));
+            const float qdz = fmaf(B.w, dx, fmaf(Q.x, dy, Q.y * dz));
             const float qd2 = fmaf(dx, qdx, fmaf(dy, qdy, dz * qdz));
             const float ir = rsqrtf(r2);
             const float ir2 = ir * ir;
             const float ir5 = ir2 * ir2 * ir;
-            const float c2 = 2.5f * qd2 * (ir5 * ir2);
-            px = fmaf(-ir5, qdx, fmaf(c2, dx, px));
-            py = fmaf(-ir5, qdy, fmaf(c2, dy, py));
-            pz = fmaf(-ir5, qdz, fmaf(c2, dz, pz));
+            // monopole and the radial quadrupole term share one multiplier of d
+            const float c = fm + 2.5f * qd2 * (ir5 * ir2);
+            px = fmaf(-ir5, qdx, fmaf(c, dx, px));
+            py = fmaf(-ir5, qdy, fmaf(c, dy, py));
+            pz = fmaf(-ir5, qdz, fmaf(c, dz, pz));
+        } else {
+            px = fmaf(fm, dx, px);
+            py = fmaf(fm, dy, py);
+            pz = fmaf(fm, dz, pz);
         }
     }
     accumulate<SPLIT>(g, px, py, pz);
@@ -514,7 +515,7 @@ __global__ void __launch_bounds__(kEvalThreads, 7) eval_kernel(NodeArrays T, Cou
                         sm.farA[lane] = rA;
                         if (QUAD) {
                             sm.farB[lane] = B;
-                            sm.farQ[lane] = D.w;
+                            sm.farQ[lane] = make_float2(D.w, -(B.x + B.y));
                         }
                     }
                     __syncwarp();
