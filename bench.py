@@ -297,12 +297,12 @@ def hbm_peak():
 
 
 def sort_roofline(st, n, split):
-    """The HBM-bound part of the tree build: the LSD radix sort (8 passes of
-    8-bit digits; each reads and writes 8 B keys + 4 B slots) and the
+    """The HBM-bound part of the tree build: the LSD radix sort (7 passes of
+    9-bit digits; each reads and writes 8 B keys + 4 B slots) and the
     permutation of the state into key order (split: pos, plo, vel, vlo, acc
     read and written, id moved, the permutation read), algorithmic bytes over
     the phase's event time."""
-    per = 8 * 24 + ((5 * 16 + 4 + 4) + (5 * 16 + 4) if split else (3 * 16 + 4 + 4) + (3 * 16 + 4))
+    per = 7 * 24 + ((5 * 16 + 4 + 4) + (5 * 16 + 4) if split else (3 * 16 + 4 + 4) + (3 * 16 + 4))
     ms = st["ms_sort"]
     peak, src = hbm_peak()
     ach = per * n / (ms * 1e-3) / 1e9 if ms > 0 else None

@@ -3,8 +3,9 @@
 //
 // One force evaluation enqueues, on the context's stream:
 //   reset counters -> bounding box + root cube -> 63-bit keys -> radix sort
-//   (8 passes) -> gather the state into key order -> tree levels 0..20 ->
-//   leaf list -> upward moments -> grouped walk (+ closing kick)
+//   (7 passes of 9-bit digits) -> gather the state into key order -> tree
+//   levels 0..20 -> leaf list -> upward moments -> grouped walk (+ closing
+//   kick)
 // then synchronises once and reads the device status word.  A node-pool or
 // walk-stack overflow is reported by the kernels (never silently dropped, as
 // the reference's GL path does at GpuBarnesHut.cpp:259-260 and :428), the
@@ -89,7 +90,7 @@ int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
     NG_CUDA(dalloc(S.keys, c)); NG_CUDA(dalloc(S.keys_alt, c)); NG_CUDA(dalloc(S.vals, c));
     NG_CUDA(dalloc(S.vals_alt, c));
     const long long nb = (c + 4095) / 4096;
-    S.hist_cap = nb * 256;
+    S.hist_cap = nb * kRsBins;
     NG_CUDA(dalloc(S.hist, S.hist_cap));
     S.scan_tmp_cap = scan_tmp_size(std::max(S.hist_cap, c)) + 16;
     NG_CUDA(dalloc(S.scan_tmp, S.scan_tmp_cap));
@@ -213,7 +214,7 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     ctx->launches += launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->F, ctx->SB.ktab, ctx->SB.keys,
                                  ctx->SB.vals, s) - 1;
     rec(ctx, 1);
-    const int passes = 8;
+    const int passes = kRsPasses;
     radix_sort_pairs(ctx->SB, n, passes, s);
     launch_permute(P, ctx->SB.vals, n, split, s);
     // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,

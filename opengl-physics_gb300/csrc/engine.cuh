@@ -24,6 +24,9 @@ namespace ngrav {
 constexpr int kKeyLevels = 21;          // 63-bit keys: 3 bits per level
 constexpr int kKeyTabLevels = 14;       // key levels whose centres are tabulated per build
 constexpr int kKeyTabSize = 1 << kKeyTabLevels;  // table entries per axis (entry 0 unused)
+constexpr int kRsDigitBits = 9;         // radix sort digit: 7 passes over the 63-bit keys
+constexpr int kRsBins = 1 << kRsDigitBits;
+constexpr int kRsPasses = (3 * kKeyLevels + kRsDigitBits - 1) / kRsDigitBits;
 constexpr int kMaxLevels = kKeyLevels + 1;
 
 // Device status word bits (sticky within one force evaluation).
@@ -155,7 +158,7 @@ struct SortBuffers {
     unsigned long long* keys_alt = nullptr;
     unsigned* vals = nullptr;
     unsigned* vals_alt = nullptr;
-    unsigned* hist = nullptr;         // 256 x blocks
+    unsigned* hist = nullptr;         // kRsBins x blocks
     unsigned* scan_tmp = nullptr;
     long long hist_cap = 0;
     long long scan_tmp_cap = 0;
@@ -255,7 +258,7 @@ void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s
 // the centre table ktab (3 * kKeyTabSize doubles).  Returns the launches made.
 int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
-// Stable LSD radix sort of (keys, vals) over bits [0, 8*passes); result ends
+// Stable LSD radix sort of (keys, vals) over bits [0, kRsDigitBits*passes); result ends
 // in (keys, vals) (the alternates are scratch).
 void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s);
 void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);

@@ -469,7 +469,8 @@ void device_exclusive_scan(const unsigned* in, unsigned* out, long long n, unsig
 }
 
 // ---------------------------------------------------------------------------
-// Stable LSD radix sort, 8-bit digits, 4096-key tiles
+// Stable LSD radix sort, 9-bit digits (seven passes cover the 63-bit keys),
+// 4096-key tiles
 // ---------------------------------------------------------------------------
 
 constexpr int kRsThreads = 256;
@@ -477,24 +478,28 @@ constexpr int kRsWarps = kRsThreads / 32;
 constexpr int kRsItems = 16;
 constexpr int kRsTile = kRsThreads * kRsItems;   // 4096
 constexpr int kRsWarpSpan = 32 * kRsItems;       // 512 consecutive keys per warp
+constexpr unsigned kRsMask = kRsBins - 1;
+static_assert(kRsBins == 2 * kRsThreads, "two digits per thread in the digit scans");
 
 // Histogram of one digit per tile, digit-major: hist[d * nblocks + b].
 __global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const unsigned long long* __restrict__ keys,
                                                              long long n, int shift, unsigned* __restrict__ hist) {
-    __shared__ unsigned h[256];
+    __shared__ unsigned h[kRsBins];
     h[threadIdx.x] = 0;
+    h[threadIdx.x + kRsThreads] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long long base = blockIdx.x * (long long)kRsTile + w * kRsWarpSpan + lane;
 #pragma unroll 4
     for (int k = 0; k < kRsItems; ++k) {
         const long long i = base + k * 32;
-        const unsigned d = i < n ? (unsigned)(keys[i] >> shift) & 255u : 256u;
+        const unsigned d = i < n ? (unsigned)(keys[i] >> shift) & kRsMask : (unsigned)kRsBins;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (d < 256u && (__ffs(peers) - 1) == lane) atomicAdd(&h[d], (unsigned)__popc(peers));
+        if (d < (unsigned)kRsBins && (__ffs(peers) - 1) == lane) atomicAdd(&h[d], (unsigned)__popc(peers));
     }
     __syncthreads();
     hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+    hist[(threadIdx.x + kRsThreads) * gridDim.x + blockIdx.x] = h[threadIdx.x + kRsThreads];
 }
 
 __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned long long* __restrict__ kin,
@@ -505,13 +510,13 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
     extern __shared__ unsigned long long rs_smem[];
     unsigned long long* skeys = rs_smem;                          // kRsTile
     unsigned* svals = reinterpret_cast<unsigned*>(skeys + kRsTile);  // kRsTile
-    __shared__ unsigned warp_cnt[kRsWarps][256];
-    __shared__ unsigned digit_start[256];   // block-local exclusive prefix over digits
-    __shared__ unsigned digit_base[256];    // global output offset of (digit, block)
+    __shared__ unsigned warp_cnt[kRsWarps][kRsBins];
+    __shared__ unsigned digit_start[kRsBins];   // block-local exclusive prefix over digits
+    __shared__ unsigned digit_base[kRsBins];    // global output offset of (digit, block)
     __shared__ unsigned s_warp[32];
 
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k = threadIdx.x; k < kRsWarps * 256; k += kRsThreads) (&warp_cnt[0][0])[k] = 0;
+    for (int k = threadIdx.x; k < kRsWarps * kRsBins; k += kRsThreads) (&warp_cnt[0][0])[k] = 0;
     __syncthreads();
 
     const long long tile = blockIdx.x * (long long)kRsTile;
@@ -526,7 +531,7 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
         const bool valid = i < n;
         key[k] = valid ? kin[i] : 0ull;
         val[k] = valid ? vin[i] : 0u;
-        const unsigned d = valid ? (unsigned)(key[k] >> shift) & 255u : 256u;
+        const unsigned d = valid ? (unsigned)(key[k] >> shift) & kRsMask : (unsigned)kRsBins;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         unsigned before = 0;
         if (valid) before = warp_cnt[w][d];
@@ -538,25 +543,30 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
         __syncwarp();
     }
     __syncthreads();
-    // Per digit: exclusive prefix over warps (stable: warp w precedes w+1).
-    const unsigned d = threadIdx.x;
-    unsigned run = 0;
+    // Per digit (thread t: digits 2t, 2t+1): exclusive prefix over warps
+    // (stable: warp w precedes w+1), then over digits.
+    const unsigned d0 = 2 * threadIdx.x, d1 = d0 + 1;
+    unsigned run0 = 0, run1 = 0;
 #pragma unroll
     for (int ww = 0; ww < kRsWarps; ++ww) {
-        const unsigned c = warp_cnt[ww][d];
-        warp_cnt[ww][d] = run;
-        run += c;
+        const unsigned c0 = warp_cnt[ww][d0], c1 = warp_cnt[ww][d1];
+        warp_cnt[ww][d0] = run0;
+        warp_cnt[ww][d1] = run1;
+        run0 += c0;
+        run1 += c1;
     }
     unsigned total;
-    const unsigned ds = block_exclusive_scan(run, s_warp, total);
-    digit_start[d] = ds;
-    digit_base[d] = hist_scan[d * gridDim.x + blockIdx.x];
+    const unsigned ds = block_exclusive_scan(run0 + run1, s_warp, total);
+    digit_start[d0] = ds;
+    digit_start[d1] = ds + run0;
+    digit_base[d0] = hist_scan[d0 * gridDim.x + blockIdx.x];
+    digit_base[d1] = hist_scan[d1 * gridDim.x + blockIdx.x];
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kRsItems; ++k) {
         const long long i = base + k * 32;
         if (i < n) {
-            const unsigned dd = (unsigned)(key[k] >> shift) & 255u;
+            const unsigned dd = (unsigned)(key[k] >> shift) & kRsMask;
             const unsigned r = digit_start[dd] + warp_cnt[w][dd] + rank[k];
             skeys[r] = key[k];
             svals[r] = val[k];
@@ -567,7 +577,7 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
     if (nvalid > kRsTile) nvalid = kRsTile;
     for (int j = threadIdx.x; j < nvalid; j += kRsThreads) {
         const unsigned long long kk = skeys[j];
-        const unsigned dd = (unsigned)(kk >> shift) & 255u;
+        const unsigned dd = (unsigned)(kk >> shift) & kRsMask;
         const unsigned o = digit_base[dd] + (unsigned)j - digit_start[dd];
         kout[o] = kk;
         vout[o] = svals[j];
@@ -588,9 +598,9 @@ void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s) 
     unsigned* vin = sb.vals;
     unsigned* vout = sb.vals_alt;
     for (int p = 0; p < passes; ++p) {
-        const int shift = 8 * p;
+        const int shift = kRsDigitBits * p;
         rs_hist_kernel<<<nb, kRsThreads, 0, s>>>(kin, n, shift, sb.hist);
-        device_exclusive_scan(sb.hist, sb.hist, (long long)nb * 256, sb.scan_tmp, s);
+        device_exclusive_scan(sb.hist, sb.hist, (long long)nb * kRsBins, sb.scan_tmp, s);
         rs_scatter_kernel<<<nb, kRsThreads, smem, s>>>(kin, vin, kout, vout, n, shift, sb.hist);
         unsigned long long* tk = kin;
         kin = kout;
