@@ -388,12 +388,17 @@ __global__ void __launch_bounds__(128) moments_kernel(NodeArrays T, Counters* C,
     }
 }
 
-// Internal nodes of one level, from their (finished) children, in FP64: mass,
-// COM (sum m x / M), traceless quadrupole by the parallel-axis shift
-// (Tree.cpp:235-251) and maxRadius = max over children of
-// maxR_c + |com_c - com| (Tree.cpp:194-201; massless nodes keep 0).  The
-// geometric opening test reads maxRadius of leaves only; the learned one reads
-// it for every node.
+// Internal nodes of one level, from their (finished) children: mass and COM
+// (sum m x / M) in FP64 in child order, as the reference's sequential sums;
+// the traceless quadrupole by the parallel-axis shift (Tree.cpp:235-251) and
+// maxRadius = max over children of maxR_c + |com_c - com| (Tree.cpp:194-201;
+// massless nodes keep 0).  GB300's FP64 pipe is narrow, so the per-child
+// work runs on the FP32 pipe from the children's walk records: offsets from
+// the double-float parent COM, the quadrupole shift summed in FP32 (the walk
+// evaluates quadrupoles in FP32), and maxRadius screened in FP32 with only
+// the children within rounding of the FP32 maximum re-measured in FP64.  The
+// geometric opening test reads maxRadius of leaves only; the learned one
+// reads it for every node.
 __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, const Counters* __restrict__ C, int l,
                                                               int quadrupole) {
     const int begin = C->level_begin[l];
@@ -429,23 +434,44 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
             pcy = py * inv;
             pcz = pz * inv;
         }
-        double PQ[5] = {0, 0, 0, 0, 0};
-        double mr = 0.0;
+        const float phx = (float)pcx, phy = (float)pcy, phz = (float)pcz;
+        const float plx = (float)(pcx - (double)phx), ply = (float)(pcy - (double)phy),
+                    plz = (float)(pcz - (double)phz);
+        float q0 = 0.f, q1 = 0.f, q2 = 0.f, q3 = 0.f, q4 = 0.f;
+        float cand[8];
+        float best = 0.f;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            if (k >= nch) break;
+            cand[k] = -1.f;
+            if (k >= nch) continue;
             const int c = fc + k;
-            const double dx = cxs[k] - pcx, dy = cys[k] - pcy, dz = czs[k] - pcz;
-            const double d2 = dx * dx + dy * dy + dz * dz;
+            const float4 A = T.wA[c], D = T.wD[c];
+            const float dx = (A.x - phx) + (D.x - plx), dy = (A.y - phy) + (D.y - ply),
+                        dz = (A.z - phz) + (D.z - plz);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             if (quadrupole && mc[k] > 0.0) {
-                PQ[0] += T.quad[5 * c + 0] + mc[k] * (3.0 * dx * dx - d2);
-                PQ[1] += T.quad[5 * c + 1] + mc[k] * (3.0 * dy * dy - d2);
-                PQ[2] += T.quad[5 * c + 2] + mc[k] * 3.0 * dx * dy;
-                PQ[3] += T.quad[5 * c + 3] + mc[k] * 3.0 * dx * dz;
-                PQ[4] += T.quad[5 * c + 4] + mc[k] * 3.0 * dy * dz;
+                const float4 B = T.wB[c];
+                const float m = A.w;
+                q0 += B.x + m * (3.f * dx * dx - d2);
+                q1 += B.y + m * (3.f * dy * dy - d2);
+                q2 += B.z + m * 3.f * dx * dy;
+                q3 += B.w + m * 3.f * dx * dz;
+                q4 += D.w + m * 3.f * dy * dz;
             }
-            if (PM > 0.0) mr = fmax(mr, T.maxr[c] + sqrt(d2));
+            cand[k] = T.wC[c].x + sqrtf(d2);  // >= maxR_c (rounded up) + |d| within FP32 rounding
+            best = fmaxf(best, cand[k]);
         }
+        double mr = 0.0;
+        if (PM > 0.0) {
+            const float cut = best * (1.f - 1e-5f) - 1e-30f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k >= nch || cand[k] < cut) continue;
+                const double dx = cxs[k] - pcx, dy = cys[k] - pcy, dz = czs[k] - pcz;
+                mr = fmax(mr, T.maxr[fc + k] + sqrt(dx * dx + dy * dy + dz * dz));
+            }
+        }
+        const double PQ[5] = {q0, q1, q2, q3, q4};
         T.mass[node] = PM;
         T.comx[node] = pcx;
         T.comy[node] = pcy;
