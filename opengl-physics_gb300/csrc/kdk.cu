@@ -676,16 +676,35 @@ double run_fma_probe(int sm_count, cudaStream_t s) {
     return 2.0 * fmas / (best * 1e-3) / 1e12;
 }
 
-// FP32 pairs, tiled: a block holds 256 targets (one per thread) and streams
-// one contiguous share of the sources through shared memory; each source tile
-// is summed in FP32 and added to the thread's FP64 totals.  Partial sums per
-// (share, target) are reduced in share order by sampler_reduce_kernel.  The
-// self pair needs no test: its separation is exactly zero, so it adds zero
-// (with eps > 0, and for the spline, whose factor is 0 at r = 0); only the
-// unsoftened Plummer form masks r = 0.
+// FP32 pairs, tiled: a block holds 512 targets (two per thread, sharing each
+// source read from shared memory) and streams one contiguous share of the
+// sources through shared memory; each source tile is summed in FP32 and added
+// to the thread's FP64 totals.  Partial sums per (share, target) are reduced
+// in share order by sampler_reduce_kernel.  The self pair needs no test: its
+// separation is exactly zero, so it adds zero (with eps > 0, and for the
+// spline, whose factor is 0 at r = 0); only the unsoftened Plummer form
+// (MASK0) masks r = 0.
 constexpr int kSampTile = 256;
+constexpr int kSampBlockTargets = 2 * kSampTile;
 
-template <int SOFT, bool SPLIT>
+template <int SOFT, bool SPLIT, bool MASK0>
+__device__ __forceinline__ void samp_pair(const float4& p, const float4& l, const float4& t, const float4& tl,
+                                          float eps2, float ih, float& px, float& py, float& pz) {
+    float dx = p.x - t.x, dy = p.y - t.y, dz = p.z - t.z;
+    if (SPLIT) {
+        dx += l.x - tl.x;
+        dy += l.y - tl.y;
+        dz += l.z - tl.z;
+    }
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float f = pair_factor<SOFT>(r2, p.w, eps2, ih);
+    if (MASK0) f = r2 > 0.f ? f : 0.f;
+    px = fmaf(f, dx, px);
+    py = fmaf(f, dy, py);
+    pz = fmaf(f, dz, pz);
+}
+
+template <int SOFT, bool SPLIT, bool MASK0>
 __global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, const float4* __restrict__ pos,
                                                                  const float4* __restrict__ plo,
                                                                  const int* __restrict__ slots, int nslots,
@@ -693,49 +712,46 @@ __global__ void __launch_bounds__(kSampTile) sampler_tiled_kernel(long long n, c
                                                                  double* __restrict__ partial) {
     __shared__ float4 sp[kSampTile];
     __shared__ float4 sl[SPLIT ? kSampTile : 1];
-    const int t = blockIdx.x * kSampTile + threadIdx.x;
-    const bool valid = t < nslots;
-    const int ti = valid ? slots[t] : -1;
+    const int t0 = blockIdx.x * kSampBlockTargets + threadIdx.x, t1 = t0 + kSampTile;
+    const bool v0 = t0 < nslots, v1 = t1 < nslots;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 tp = valid ? pos[ti] : zero;
-    const float4 tl = (valid && SPLIT) ? plo[ti] : zero;
-    const bool mask0 = SOFT == kSoftPlummer && !(eps2 > 0.f);
+    const float4 ta = v0 ? pos[slots[t0]] : zero, tb = v1 ? pos[slots[t1]] : zero;
+    const float4 tla = (v0 && SPLIT) ? plo[slots[t0]] : zero, tlb = (v1 && SPLIT) ? plo[slots[t1]] : zero;
     const long long j0 = (long long)blockIdx.y * share;
     const long long j1 = j0 + share < n ? j0 + share : n;
-    double ax = 0.0, ay = 0.0, az = 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0, bx = 0.0, by = 0.0, bz = 0.0;
     for (long long base = j0; base < j1; base += kSampTile) {
         const long long j = base + threadIdx.x;
         sp[threadIdx.x] = j < j1 ? pos[j] : zero;
         if (SPLIT) sl[threadIdx.x] = j < j1 ? plo[j] : zero;
         __syncthreads();
         const int cnt = (int)(j1 - base < kSampTile ? j1 - base : kSampTile);
-        float px = 0.f, py = 0.f, pz = 0.f;
+        float pax = 0.f, pay = 0.f, paz = 0.f, pbx = 0.f, pby = 0.f, pbz = 0.f;
         for (int k = 0; k < cnt; ++k) {
             const float4 p = sp[k];
-            float dx = p.x - tp.x, dy = p.y - tp.y, dz = p.z - tp.z;
-            if (SPLIT) {
-                const float4 l = sl[k];
-                dx += l.x - tl.x;
-                dy += l.y - tl.y;
-                dz += l.z - tl.z;
-            }
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            float f = pair_factor<SOFT>(r2, p.w, eps2, ih);
-            if (mask0) f = r2 > 0.f ? f : 0.f;
-            px = fmaf(f, dx, px);
-            py = fmaf(f, dy, py);
-            pz = fmaf(f, dz, pz);
+            const float4 l = SPLIT ? sl[k] : zero;
+            samp_pair<SOFT, SPLIT, MASK0>(p, l, ta, tla, eps2, ih, pax, pay, paz);
+            samp_pair<SOFT, SPLIT, MASK0>(p, l, tb, tlb, eps2, ih, pbx, pby, pbz);
         }
-        ax += px;
-        ay += py;
-        az += pz;
+        ax += pax;
+        ay += pay;
+        az += paz;
+        bx += pbx;
+        by += pby;
+        bz += pbz;
         __syncthreads();
     }
-    if (valid) {
-        double* o = partial + ((long long)blockIdx.y * nslots + t) * 3;
+    if (v0) {
+        double* o = partial + ((long long)blockIdx.y * nslots + t0) * 3;
         o[0] = ax;
         o[1] = ay;
         o[2] = az;
+    }
+    if (v1) {
+        double* o = partial + ((long long)blockIdx.y * nslots + t1) * 3;
+        o[0] = bx;
+        o[1] = by;
+        o[2] = bz;
     }
 }
 
@@ -749,7 +765,7 @@ __global__ void sampler_reduce_kernel(const double* __restrict__ partial, int ns
 }
 
 int sampler_shares(long long n, int nslots, int sm_count) {
-    const int tb = (nslots + kSampTile - 1) / kSampTile;
+    const int tb = (nslots + kSampBlockTargets - 1) / kSampBlockTargets;
     long long sh = ((long long)sm_count * 4 + tb - 1) / tb;
     const long long max_sh = (n + kSampTile - 1) / kSampTile;
     if (sh > max_sh) sh = max_sh;
@@ -765,23 +781,22 @@ void launch_sampler(long long n, const Particles& P, bool split, const int* slot
     }
     long long share = (n + shares - 1) / shares;
     share = (share + kSampTile - 1) / kSampTile * kSampTile;
-    const dim3 grid((nslots + kSampTile - 1) / kSampTile, shares);
+    const dim3 grid((nslots + kSampBlockTargets - 1) / kSampBlockTargets, shares);
     const float ih = spline_h > 0.0 ? (float)(1.0 / spline_h) : 0.f;
+    const float4* lo = split ? P.plo : nullptr;
+#define NGRAV_SAMP(SOFT, SP, M0) \
+    sampler_tiled_kernel<SOFT, SP, M0><<<grid, kSampTile, 0, s>>>(n, P.pos, lo, slots, nslots, (float)eps2, ih, share, partial)
     if (spline_h > 0.0) {
-        if (split)
-            sampler_tiled_kernel<kSoftSpline, true><<<grid, kSampTile, 0, s>>>(n, P.pos, P.plo, slots, nslots, 0.f, ih,
-                                                                              share, partial);
-        else
-            sampler_tiled_kernel<kSoftSpline, false><<<grid, kSampTile, 0, s>>>(n, P.pos, nullptr, slots, nslots, 0.f,
-                                                                               ih, share, partial);
+        if (split) NGRAV_SAMP(kSoftSpline, true, false);
+        else NGRAV_SAMP(kSoftSpline, false, false);
+    } else if (eps2 > 0.0) {
+        if (split) NGRAV_SAMP(kSoftPlummer, true, false);
+        else NGRAV_SAMP(kSoftPlummer, false, false);
     } else {
-        if (split)
-            sampler_tiled_kernel<kSoftPlummer, true><<<grid, kSampTile, 0, s>>>(n, P.pos, P.plo, slots, nslots,
-                                                                                (float)eps2, 0.f, share, partial);
-        else
-            sampler_tiled_kernel<kSoftPlummer, false><<<grid, kSampTile, 0, s>>>(n, P.pos, nullptr, slots, nslots,
-                                                                                 (float)eps2, 0.f, share, partial);
+        if (split) NGRAV_SAMP(kSoftPlummer, true, true);
+        else NGRAV_SAMP(kSoftPlummer, false, true);
     }
+#undef NGRAV_SAMP
     sampler_reduce_kernel<<<(3 * nslots + 255) / 256, 256, 0, s>>>(partial, nslots, shares, out);
 }
 

@@ -63,6 +63,29 @@ def test_force_error_sampler_matches_oracle(pkg, oracle, fp64_pairs):
     assert fe["median"] <= np.quantile(e_all, 0.75)
 
 
+@pytest.mark.parametrize("case", ["plummer", "eps0", "spline", "plain"])
+def test_fp32_pair_sampler_matches_fp64_pairs(pkg, ic, case):
+    """The tiled FP32-pair sampler (two targets per thread, FP64 tile sums)
+    against the FP64-pair sampler on the same drawn targets: the error
+    statistics agree to the FP32 rounding of the reference forces.  Covers
+    every instance: softened Plummer, eps = 0 (self pair masked), spline,
+    plain precision; 1,500 targets leave the second block half full."""
+    x, y, z, vx, vy, vz, m = ic.plummer(20000, seed=4)
+    eps = 0.0 if case == "eps0" else 0.01
+    prec = pkg.PRECISION_PLAIN if case == "plain" else pkg.PRECISION_SPLIT
+    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=0.6), leaf_capacity=16, precision=prec) as sim:
+        if case == "spline":
+            sim.set_softening(pkg.SOFTENING_SPLINE)
+        sim.set_particles(x, y, z, vx, vy, vz, m)
+        sim.compute_accel()
+        f32 = sim.force_error(1500, seed=21, fp64_pairs=False)
+        f64 = sim.force_error(1500, seed=21, fp64_pairs=True)
+    assert f32["nsample"] == f64["nsample"] == 1500
+    assert np.isfinite(f32["rms"]) and f32["rms"] > 0
+    for k in ("rms", "max", "median"):
+        assert f32[k] == pytest.approx(f64[k], rel=1e-3, abs=1e-6), (k, f32[k], f64[k])
+
+
 def test_momentum_and_com_drift_small(pkg, ic):
     x, y, z, vx, vy, vz, m = ic.plummer(32768, seed=2)
     with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=0.01, theta=0.5, dt=1e-3), leaf_capacity=16) as sim:
