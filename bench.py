@@ -27,6 +27,9 @@ e2e     = the same metric through the C-ABI with host buffers: per step
 roofline: the evaluation kernel (P2P + P2C, FP32 pipe): algorithmic
           flops (20 per P2P pair + 60 per P2C term, device-counted) / its
           event-timed duration, against the measured FP32 FMA peak.
+roofline_p2p: the evaluation kernel's P2P phase alone (a 262,144-particle
+          Plummer sphere at theta 0: every pair near, no P2C), 20 flops per
+          pair over its event time, against the same FP32 peak.
 roofline_sort: the HBM-bound part of the tree build (radix sort + the
           permutation into key order), algorithmic bytes / event time of
           that phase, against the measured copy bandwidth.
@@ -311,6 +314,30 @@ def sort_roofline(st, n, split):
             "peak_source": src}
 
 
+def p2p_phase_roofline(pkg, ic, dev, peak, prec):
+    """The evaluation kernel's P2P phase on its own: a Plummer sphere of
+    262,144 particles at theta = 0, where the walk opens every node, so every
+    interaction is a near-field pair (no P2C term); 20 algorithmic flops per
+    pair over the kernel's event time (best of three evaluations), against
+    the measured FP32 peak."""
+    arrs = ic.plummer(262144, seed=5)
+    best = None
+    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=0.01, theta=0.0), leaf_capacity=32, precision=prec,
+                         device=dev, timing=True) as s:
+        s.set_particles_f32(*arrs)
+        for _ in range(3):
+            s.compute_accel()
+            st = s.stats()
+            if best is None or st["ms_force"] < best[0]:
+                best = (st["ms_force"], st["p2p_pairs"], st["p2c_terms"])
+    ms, pairs, terms = best
+    ach = 20.0 * pairs / (ms * 1e-3) / 1e12 if ms > 0 else None
+    return {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak if ach and peak else None, "kernel": "eval_kernel, P2P only (20 flops/pair)",
+            "workload": "Plummer N=262144, theta 0 (all pairs near), leaf capacity 32", "p2p_pairs": pairs,
+            "p2c_terms": terms, "ms": ms}
+
+
 def phases(st):
     return {k: st[k] for k in ("ms_bbox_keys", "ms_sort", "ms_build", "ms_moments", "ms_walk", "ms_force")}
 
@@ -534,6 +561,7 @@ def main():
                          "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)",
                          "peak_source": "measured FP32 FMA probe (ngrav_gpu_probe_fp32_peak)"},
             "roofline_sort": sort_roofline(st, n, args.precision == "split"),
+            "roofline_p2p": p2p_phase_roofline(pkg, ic, dev, peak, prec),
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,
         }
         print(json.dumps(line), flush=True)

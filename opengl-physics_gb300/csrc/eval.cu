@@ -14,11 +14,11 @@
 // of the group.  A group's targets run in blocks of up to 64, each in one or
 // two passes over every staged chunk (split to keep the lanes busy: 20
 // targets as 4 x 8 + 16 x 2 slices), the second pass's sums parked in shared
-// memory; 72 registers and 7.6 KiB of shared memory per warp keep 7 CTAs of
-// 4 warps per SM.  Far records are staged 32 at a time into shared memory in
+// memory; 80 registers and 8.75 KiB of shared memory per warp keep 6 CTAs
+// of 4 warps per SM.  Far records are staged 32 at a time into shared memory in
 // the group's frame, the next batch loading into registers while this one is
 // evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
-// per leaf, completing on an mbarrier with a bounded wait) into a 4 KiB
+// per leaf, completing on an mbarrier with a bounded wait) into a 5 KiB
 // shared-memory buffer, each batch as many leaves (up to 32) as fit by
 // their actual counts; the next batch's leaf records load while a batch is
 // in flight.  (A second buffer would overlap copy and compute within the
@@ -33,7 +33,7 @@ namespace ngrav {
 
 constexpr int kEvalWarps = 4;
 constexpr int kEvalThreads = kEvalWarps * 32;
-constexpr int kSrcCap = 256;                  // sources per staging buffer (4 KiB)
+constexpr int kSrcCap = 320;                  // sources per staging buffer (5 KiB)
 constexpr int kBuffers = 1;                   // staging buffers per warp (2 halves occupancy)
 constexpr unsigned kWaitLimit = 1u << 26;     // bounded mbarrier polling
 
@@ -447,7 +447,7 @@ __device__ __forceinline__ void finish_targets(EvalSmem& sm, const Lane& g, int 
 }
 
 template <bool SPLIT, bool QUAD, int SOFT>
-__global__ void __launch_bounds__(kEvalThreads, 7) eval_kernel(NodeArrays T, Counters* C,
+__global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
                                                             float4* __restrict__ acc, float4* __restrict__ vel,
                                                             float4* __restrict__ vlo,
