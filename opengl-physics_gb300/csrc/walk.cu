@@ -83,13 +83,49 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(NodeArrays T, Counte
         // own members first (the self term is zero)
         list_append(near, lane == 0, leaf, LB.near, LB.near_next, &C->near_chunks, LB.near_chunk_cap, lane,
                     lt_mask, bad);
-        int size = 0;
+        int size = 0, visits = 0;
         const int root = T.sysroot[leaf];
         if (leaf != root) {
-            if (lane == 0) stack[0] = root;
-            size = 1;
+            // The root's test, by every lane at once (the same arithmetic as
+            // the loop's): when it opens, as it nearly always does, its
+            // children start the stack, sparing an iteration that would test
+            // one node; otherwise the root takes the loop's path.
+            const float4 A = T.wA[root], Cw = T.wC[root], D = T.wD[root];
+            const int meta = __float_as_int(Cw.w);
+            bool open = false;
+            if (A.w > 0.f && meta >= 0) {
+                const float dx = (A.x - gA.x) + (D.x - gD.x);
+                const float dy = (A.y - gA.y) + (D.y - gD.y);
+                const float dz = (A.z - gA.z) + (D.z - gD.z);
+                const float dist = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                const float worst = dist - gR;
+                const float size_n = Cw.y;
+                bool accept = worst > 0.f && size_n * size_n < wp.theta2 * worst * worst;
+                if (wp.retest) {
+                    const float margin = wp.theta * worst - size_n;
+                    if (fabsf(margin) <= 1e-5f * (wp.theta * (dist + gR) + size_n)) {
+                        if (lane == 0) ++retests;
+                        const double ex = T.comx[root] - gcx_d, ey = T.comy[root] - gcy_d,
+                                     ez = T.comz[root] - gcz_d;
+                        const double d2 = ex * ex + ey * ey + ez * ez;
+                        const double sz = 2.0 * T.half[root];
+                        const double w = sqrt(d2) - gr_d;
+                        accept = w > 0.0 && sz * sz < wp.theta2_d * w * w;
+                    }
+                }
+                open = !accept;
+            }
+            if (open) {
+                const int nch = meta & 0xFFFFFF, link = __float_as_int(Cw.z);
+                if (lane < nch) stack[lane] = link + lane;
+                size = nch;
+                visits = 1;
+                tests += 1;
+            } else {
+                if (lane == 0) stack[0] = root;
+                size = 1;
+            }
         }
-        int visits = 0;
         __syncwarp();
         while (size > 0) {
             const int take = min(size, 32 * kNPL);

@@ -152,9 +152,32 @@ __global__ void __launch_bounds__(kLwThreads, MINB) walk_lmac_round_kernel(NodeA
                         lt_mask, bad);
             const int root = T.sysroot[leaf];
             if (leaf != root) {
-                if (lane == 0) stack[0] = root;
-                size = 1;
+                // The root's first rule (open when worst <= 0 or 2h >= rho_hi
+                // worst), by every lane at once: when it opens, as it nearly
+                // always does, its children start the stack, sparing an
+                // iteration that would test one node; otherwise the root takes
+                // the loop's path.
+                const float4 A = T.wA[root], Cw = T.wC[root], D = T.wD[root];
+                const int meta = __float_as_int(Cw.w);
+                bool open = false;
+                if (A.w > 0.f && meta >= 0) {
+                    const float dx = (A.x - gA.x) + (D.x - gD.x);
+                    const float dy = (A.y - gA.y) + (D.y - gD.y);
+                    const float dz = (A.z - gA.z) + (D.z - gD.z);
+                    const float worst = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) - gR;
+                    open = !(worst > 0.f) || Cw.y >= wp.lm_rho_hi * worst;
+                }
+                if (open) {
+                    const int nch = meta & 0xFFFFFF, link = __float_as_int(Cw.z);
+                    if (lane < nch) stack[lane] = link + lane;
+                    size = nch;
+                    tests += 1;
+                } else {
+                    if (lane == 0) stack[0] = root;
+                    size = 1;
+                }
             }
+            __syncwarp();
         } else {
             const LmacGroupState g = R.gs[gi];
             far = {g.far_first, g.far_cur, g.far_pos, g.far_count, fres_next, fres_end};
