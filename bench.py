@@ -15,7 +15,8 @@ Setup, untimed: for each leaf capacity of --leaf-grid (the target-group
 size), the network is trained on the run itself (16 snapshots, 2^22
 labelled pairs), and theta and the learned budget are each set to the
 largest grid value whose error stays within the target; each arm then runs
-at the leaf capacity whose calibrated evaluation is fastest.  Both arms
+at the leaf capacity whose calibrated evaluation is fastest, with the
+faster of the two walk-stack sizes.  Both arms
 step the same input state K times.
 
 value   = N * K / (device time of the learned arm's K timed steps, CUDA
@@ -446,13 +447,26 @@ def main():
         dist.barrier()
     clocks = ClockSampler(dev)
 
+    def pick_walk_stack():
+        """The arm's per-warp walk stack (2,048 entries at 6 CTAs per SM, or
+        1,024 at 8): the faster evaluation of this state, installed."""
+        ms = {}
+        for ws in (2048, 1024):
+            sim.set_tuning(0, ws)
+            ms[ws] = eval_ms(reps=5)
+        best = min(ms, key=ms.get)
+        sim.set_tuning(0, best)
+        return best
+
     # ---- geometric (plain theta) arm ----
     restart(ncrit_t)
     sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
+    ws_t = pick_walk_stack()
     st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks, dist)
     ms_g = replica_max(ms_g, dist, f"cuda:{dev}")
     fe_g = error_at(sim)
-    arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "value": job_value(n, world, ms_g), "ms_per_step": ms_g,
+    arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "walk_stack": ws_t, "value": job_value(n, world, ms_g),
+                 "ms_per_step": ms_g,
                  "force_err_rms": fe_g["rms"], "force_err_max": fe_g["max"],
                  "p2p_pairs_per_step": st_g["cum_p2p_pairs"] / max(1, st_g["cum_evals"]),
                  "p2c_terms_per_step": st_g["cum_p2c_terms"] / max(1, st_g["cum_evals"]),
@@ -461,11 +475,13 @@ def main():
                  "ms_phases_last_eval": phases(st_g), "calibration": cal_theta}
 
     # ---- learned arm (the method) ----
+    ws_l = ws_t
     if learned:
         restart(ncrit_l)
         sim.lmac_set_model(*best_l["model"])
         sim.set_opts(theta=best_l["theta"], mac=pkg.MAC_LEARNED)
         sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=TARGET_RMS * 1.5)
+        ws_l = pick_walk_stack()
         sim.lmac_reset()
         st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks, dist)
         fe = error_at(sim)
@@ -524,6 +540,7 @@ def main():
     if rank == 0:
         cfg = {"workload": args.workload, "n": n, "mac": args.mac, "eps": eps, "dt": dt,
                "leaf_capacity": ncrit_l if learned else ncrit_t, "leaf_capacity_tuning": tuning_table,
+               "walk_stack": ws_l if learned else ws_t,
                "precision": args.precision, "quadrupole": True, "target_rms": TARGET_RMS,
                "parallelism": "replicas" if world > 1 else "single-gpu",
                "l2": "per-step working set > 0.5 GB, larger than the 129 MB L2",
