@@ -264,13 +264,18 @@ int ngrav_gpu_probe_fp32_peak(int device, double* tflops);
  * cudaMalloc/cudaFree (and cudaFree's device-wide synchronisation) out of
  * its frame loop.  No reference counterpart.
  *   x..m        caller-owned DEVICE arrays of n FP32 values on `device`
- *   with_potential  1: also the exact O(N^2) FP64 pair potential (G, eps)
+ *   with_potential  1: also the exact O(N^2) FP64 Plummer pair potential
+ *               (G, eps; Plummer softening only, whatever softening a context
+ *               uses).  It costs n^2/2 FP64 pair terms: about 1 s at
+ *               n = 262,144 on one GB300, above an hour at the maximum n.
+ *               0: potential and energy are NaN, as in ngrav_gpu_diagnostics.
  *   out         HOST struct, filled like ngrav_gpu_diagnostics fills it
  * Allocates nothing: its scratch is a static 256 KiB device array that every
  * GPU loading this library holds until exit.  The first call on a device
  * looks that array's address up (so make it before any stream capture).
  * Calls share the array, so calls overlapping on the GPU race; serialise
- * them.  Runs on the legacy default stream and returns when done.
+ * them.  Runs on the legacy default stream of `device` and returns when
+ * done, with the caller's current device restored.
  * Returns NGRAV_ERR_INVALID_ARG for n > NGRAV_NOALLOC_MAX_N. */
 int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const float* y, const float* z,
                                   const float* vx, const float* vy, const float* vz, const float* m, double G,

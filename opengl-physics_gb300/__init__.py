@@ -227,9 +227,11 @@ def load_library(path: str | None = None):
     return L
 
 
-def diagnostics_noalloc(device, n, x, y, z, vx, vy, vz, m, G, eps, with_potential=True):
+def diagnostics_noalloc(device, n, x, y, z, vx, vy, vz, m, G, eps, with_potential=False):
     """Conservation diagnostics of caller-owned device FP32 arrays (raw device
-    pointers as ints), allocating no device memory (see the C header)."""
+    pointers as ints), allocating no device memory (see the C header).  The
+    exact potential costs n^2/2 FP64 pair terms, so it is opt-in; without it
+    potential and energy are NaN."""
     L = load_library()
     d = Diag()
     rc = L.ngrav_gpu_diagnostics_noalloc(int(device), int(n), *[ctypes.c_void_p(int(p)) for p in

@@ -22,18 +22,31 @@
 // overlaps on the GPU (different host threads or streams) race and must be
 // serialised by the caller.  Each call overwrites every partial it reads, so
 // nothing needs clearing between calls.
+//
+// The potential is the exact O(N^2) FP64 sum of the Plummer pair potential
+// -G m_i m_j / sqrt(r^2 + eps^2) (System::TotalEnergy,
+// include/ngrav/System.hpp:119-164, with Plummer softening only).  It runs
+// as its own kernel: targets in tiles of 256 (one per thread), sources j > i
+// staged through shared memory, every block taking a light and a heavy
+// target tile of the triangle in turn so the blocks finish together.  Its
+// cost is n^2 / 2 FP64 pair terms: about 1 s at n = 262,144 on one GB300
+// (FP64 on the CUDA cores), and about 4,000 times that, above an hour, at
+// the 16,777,216-particle maximum -- ask for it only at sizes where that
+// fits.
 #include "ngrav_gpu.h"
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 namespace {
 
 constexpr int kThreads = 256;
-constexpr long long kPerBlock = 4096;                   // particles per block
+constexpr long long kPerBlock = 4096;                   // particles per block of passes 1 and 2
 constexpr int kMaxBlocks = NGRAV_NOALLOC_MAX_N / 4096;  // 4096 blocks
 constexpr int kSlots = 8;                               // doubles per block partial
+constexpr int kPotTile = kThreads;                      // potential: targets and sources per tile
 
 // kMaxBlocks rows of block partials + 2 rows of pass totals: 262,160 bytes.
 static __device__ __align__(256) double g_noalloc_scratch[(kMaxBlocks + 2) * kSlots];
@@ -79,17 +92,15 @@ __global__ void __launch_bounds__(kThreads) na_pass1(long long n, const float* _
     }
 }
 
-// Pass 2: {Lx, Ly, Lz} about the COM, plus the exact pair potential of the
-// block's targets against every later particle when with_pot is set.
+// Pass 2: {Lx, Ly, Lz} about the COM; slot 3 is zeroed for the potential pass.
 __global__ void __launch_bounds__(kThreads) na_pass2(long long n, const float* __restrict__ x,
                                                      const float* __restrict__ y, const float* __restrict__ z,
                                                      const float* __restrict__ vx, const float* __restrict__ vy,
                                                      const float* __restrict__ vz, const float* __restrict__ m,
-                                                     const double* __restrict__ com, double eps2, int with_pot,
-                                                     double* __restrict__ scratch) {
+                                                     const double* __restrict__ com, double* __restrict__ scratch) {
     __shared__ double sh[kThreads / 32];
     const double cx = com[0], cy = com[1], cz = com[2];
-    double L[3] = {0, 0, 0}, pot = 0.0;
+    double L[3] = {0, 0, 0};
     const long long lo = blockIdx.x * kPerBlock, hi = min(n, lo + kPerBlock);
     for (long long i = lo + threadIdx.x; i < hi; i += kThreads) {
         const double mi = m[i], rx = x[i] - cx, ry = y[i] - cy, rz = z[i] - cz;
@@ -97,23 +108,76 @@ __global__ void __launch_bounds__(kThreads) na_pass2(long long n, const float* _
         L[0] += mi * (ry * w - v * rz);
         L[1] += mi * (rz * u - w * rx);
         L[2] += mi * (rx * v - u * ry);
-        if (with_pot) {
-            const double xi = x[i], yi = y[i], zi = z[i];
-            double local = 0.0;
-            for (long long j = i + 1; j < n; ++j) {
-                const double dx = (double)x[j] - xi, dy = (double)y[j] - yi, dz = (double)z[j] - zi;
-                local -= (double)m[j] * rsqrt(dx * dx + dy * dy + dz * dz + eps2);
-            }
-            pot += mi * local;
-        }
     }
     const double t0 = block_sum(L[0], sh), t1 = block_sum(L[1], sh), t2 = block_sum(L[2], sh);
-    const double tp = block_sum(pot, sh);
     if (threadIdx.x == 0) {
         scratch[blockIdx.x * kSlots + 0] = t0;
         scratch[blockIdx.x * kSlots + 1] = t1;
         scratch[blockIdx.x * kSlots + 2] = t2;
-        scratch[blockIdx.x * kSlots + 3] = tp;
+        scratch[blockIdx.x * kSlots + 3] = 0.0;
+    }
+}
+
+// Sum over j > i of -m_i m_j / sqrt(r^2 + eps^2) for the targets of one
+// tile (thread = target), the sources staged kPotTile at a time.
+__device__ double pot_tile(long long n, long long t0, const float* __restrict__ x, const float* __restrict__ y,
+                           const float* __restrict__ z, const float* __restrict__ m, double eps2, double* sx,
+                           double* sy, double* sz, double* sm) {
+    const long long i = t0 + threadIdx.x;
+    double xi = 0.0, yi = 0.0, zi = 0.0, mi = 0.0;
+    if (i < n) {
+        xi = x[i];
+        yi = y[i];
+        zi = z[i];
+        mi = m[i];
+    }
+    double local = 0.0;
+    for (long long s0 = t0; s0 < n; s0 += kPotTile) {  // source tiles from the target tile on
+        const long long j = s0 + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            sx[threadIdx.x] = x[j];
+            sy[threadIdx.x] = y[j];
+            sz[threadIdx.x] = z[j];
+            sm[threadIdx.x] = m[j];
+        }
+        __syncthreads();
+        if (i < n) {
+            const int kmax = (int)min((long long)kPotTile, n - s0);
+            for (int k = 0; k < kmax; ++k) {
+                if (s0 + k <= i) continue;
+                const double dx = sx[k] - xi, dy = sy[k] - yi, dz = sz[k] - zi;
+                local -= sm[k] * rsqrt(dx * dx + dy * dy + dz * dz + eps2);
+            }
+        }
+    }
+    return mi * local;
+}
+
+// Exact pair potential.  Block b takes target tiles b, 2B-1-b, 2B+b,
+// 4B-1-b, ... of the ntiles: a tile near the start of the triangle (long)
+// with one near its end (short), so the B blocks carry about equal work.
+// Each block writes its sum to slot 3 of its own partial row; rows at or
+// past nb_l (which pass 2 did not write) get zero angular momentum.
+__global__ void __launch_bounds__(kThreads) na_potential(long long n, const float* __restrict__ x,
+                                                         const float* __restrict__ y, const float* __restrict__ z,
+                                                         const float* __restrict__ m, double eps2, int nb_l,
+                                                         double* __restrict__ scratch) {
+    __shared__ double sx[kPotTile], sy[kPotTile], sz[kPotTile], sm[kPotTile];
+    __shared__ double sh[kThreads / 32];
+    const long long ntiles = (n + kPotTile - 1) / kPotTile;
+    const long long B = gridDim.x, b = blockIdx.x;
+    double pot = 0.0;
+    for (long long base = 0; base < ntiles; base += 2 * B) {
+        const long long ta = base + b, tb = base + 2 * B - 1 - b;
+        if (ta < ntiles) pot += pot_tile(n, ta * kPotTile, x, y, z, m, eps2, sx, sy, sz, sm);
+        if (tb < ntiles) pot += pot_tile(n, tb * kPotTile, x, y, z, m, eps2, sx, sy, sz, sm);
+    }
+    const double t = block_sum(pot, sh);
+    if (threadIdx.x == 0) {
+        double* row = scratch + (size_t)blockIdx.x * kSlots;
+        if ((int)blockIdx.x >= nb_l) row[0] = row[1] = row[2] = 0.0;
+        row[3] = t;
     }
 }
 
@@ -148,14 +212,10 @@ int scratch_for_current_device(int device, double** out) {
     return NGRAV_OK;
 }
 
-}  // namespace
-
-extern "C" int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const float* y, const float* z,
-                                             const float* vx, const float* vy, const float* vz, const float* m,
-                                             double G, double eps, int with_potential, ngrav_gpu_diag* out) {
-    if (!out || n <= 0 || !x || !y || !z || !vx || !vy || !vz || !m) return NGRAV_ERR_INVALID_ARG;
-    if (n > (int64_t)NGRAV_NOALLOC_MAX_N) return NGRAV_ERR_INVALID_ARG;  // beyond the static scratch
-    if (cudaSetDevice(device) != cudaSuccess) return NGRAV_ERR_CUDA;
+// The work of one call with `device` current.
+int run_diagnostics(int device, int64_t n, const float* x, const float* y, const float* z, const float* vx,
+                    const float* vy, const float* vz, const float* m, double G, double eps, int with_potential,
+                    ngrav_gpu_diag* out) {
     double* scratch = nullptr;
     const int rc = scratch_for_current_device(device, &scratch);
     if (rc) return rc;
@@ -168,10 +228,18 @@ extern "C" int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float*
     na_pass1<<<nb, kThreads, 0, s>>>(n, x, y, z, vx, vy, vz, m, scratch);
     na_reduce<<<1, 32, 0, s>>>(nb, scratch, tot1);
     na_com<<<1, 1, 0, s>>>(tot1, tot2);
-    na_pass2<<<nb, kThreads, 0, s>>>(n, x, y, z, vx, vy, vz, m, tot2, eps * eps, with_potential ? 1 : 0, scratch);
+    na_pass2<<<nb, kThreads, 0, s>>>(n, x, y, z, vx, vy, vz, m, tot2, scratch);
+    int rows = nb;
+    if (with_potential) {
+        // one block per target tile up to the kMaxBlocks partial rows
+        // (ntiles >= nb, so every row pass 2 wrote gets its potential)
+        const long long ntiles = (n + kPotTile - 1) / kPotTile;
+        rows = (int)(ntiles < kMaxBlocks ? ntiles : kMaxBlocks);
+        na_potential<<<rows, kThreads, 0, s>>>(n, x, y, z, m, eps * eps, nb, scratch);
+    }
     double h1[kSlots];
     if (cudaMemcpy(h1, tot1, sizeof(h1), cudaMemcpyDeviceToHost) != cudaSuccess) return NGRAV_ERR_CUDA;
-    na_reduce<<<1, 32, 0, s>>>(nb, scratch, tot2);
+    na_reduce<<<1, 32, 0, s>>>(rows, scratch, tot2);
     double h2[kSlots];
     if (cudaMemcpy(h2, tot2, sizeof(h2), cudaMemcpyDeviceToHost) != cudaSuccess) return NGRAV_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return NGRAV_ERR_CUDA;
@@ -182,8 +250,27 @@ extern "C" int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float*
         out->P[k] = h1[5 + k];
         out->L[k] = h2[k];
     }
+    // Without the potential, potential and energy are NaN, as in
+    // ngrav_gpu_diagnostics, so a drift computed from them cannot pass for
+    // an energy drift.
     out->potential_exact = with_potential ? 1 : 0;
-    out->potential = with_potential ? G * h2[3] : 0.0;
+    out->potential = with_potential ? G * h2[3] : std::nan("");
     out->energy = out->kinetic + out->potential;
     return NGRAV_OK;
+}
+
+}  // namespace
+
+extern "C" int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const float* y, const float* z,
+                                             const float* vx, const float* vy, const float* vz, const float* m,
+                                             double G, double eps, int with_potential, ngrav_gpu_diag* out) {
+    if (!out || n <= 0 || !x || !y || !z || !vx || !vy || !vz || !m) return NGRAV_ERR_INVALID_ARG;
+    if (n > (int64_t)NGRAV_NOALLOC_MAX_N) return NGRAV_ERR_INVALID_ARG;  // beyond the static scratch
+    // The caller's current device is put back before returning.
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) return NGRAV_ERR_CUDA;
+    if (device != prev && cudaSetDevice(device) != cudaSuccess) return NGRAV_ERR_CUDA;
+    const int rc = run_diagnostics(device, n, x, y, z, vx, vy, vz, m, G, eps, with_potential, out);
+    if (device != prev && cudaSetDevice(prev) != cudaSuccess) return rc ? rc : NGRAV_ERR_CUDA;
+    return rc;
 }

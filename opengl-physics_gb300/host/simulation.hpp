@@ -9,10 +9,10 @@
 // stack on this system.
 #pragma once
 
-#include <fstream>
-#include <map>
+#include <cstdio>
 #include <string>
 #include <string_view>
+#include <unordered_map>
 #include <vector>
 
 namespace fw {
@@ -47,10 +47,13 @@ enum class NpyDtype { F4, F8, C8, I4 };
 
 // <dir>/deck.toml, <dir>/manifest.json, <dir>/diagnostics.csv and
 // <dir>/frames/<field>_NNNN.npy, byte-compatible with the reference's writer
-// (framework/src/OutputWriter.cpp:38-167).
+// (the format of framework/src/OutputWriter.cpp:38-167; output_writer.cpp
+// states it).  Per frame: BeginFrame, then WriteField / WriteScalar, then
+// EndFrame; Finish once at the end writes the manifest.
 class OutputWriter {
 public:
     OutputWriter(std::string outDir, const SimInfo& info, const Deck& deck);
+    ~OutputWriter();
     OutputWriter(const OutputWriter&) = delete;
     OutputWriter& operator=(const OutputWriter&) = delete;
 
@@ -59,23 +62,24 @@ public:
     void WriteScalar(std::string_view name, double value);
     void EndFrame();
     void Finish();
-    int FramesWritten() const { return m_frameIndex; }
+    // Index of the frame begun last (the reference's accessor: frames - 1).
+    int FramesWritten() const { return m_frames - 1; }
 
 private:
-    struct FieldMeta {
-        NpyDtype dtype = NpyDtype::F4;
-        int ny = 0;
-        int nx = 0;
+    struct FieldShape {             // a field's dtype and shape at its first write
+        std::string name;
+        NpyDtype dtype;
+        int ny, nx;
     };
     std::string m_dir;
     SimInfo m_info;
-    std::ofstream m_csv;
-    std::map<std::string, FieldMeta> m_fields;
-    std::map<std::string, double> m_pendingScalars;
-    int m_frameIndex = -1;
-    double m_frameT = 0.0;
-    long m_frameStep = 0;
-    bool m_finished = false;
+    std::FILE* m_csv = nullptr;
+    std::unordered_map<std::string, size_t> m_column;  // diagnostics name -> CSV column
+    std::vector<FieldShape> m_fieldLog;                // in order of first write
+    std::vector<double> m_row;                         // this frame's scalars (NaN: not written)
+    int m_frames = 0;                                  // frames begun
+    double m_t = 0.0;
+    long m_step = 0;
 };
 
 struct HeadlessOptions {

@@ -25,3 +25,13 @@ g++ -std=gnu++20 -O3 -march=native -funroll-loops -fopenmp -fPIC -shared \
     -o "$HERE/_ref/libngrav_ref.so.tmp"
 mv "$HERE/_ref/libngrav_ref.so.tmp" "$HERE/_ref/libngrav_ref.so"
 echo "build_ref: $HERE/_ref/libngrav_ref.so"
+# The reference's run-directory writer (framework/src/OutputWriter.cpp, with
+# fw::Deck and its vendored TOML parser), driven by writer_driver.cpp: the
+# source of the byte-level writer fixture.
+FW="$REF/framework"
+g++ -std=gnu++20 -O2 -DNGRAV_WRITER_REF \
+    -I "$FW/include" -I "$FW/third_party" \
+    "$FW/src/OutputWriter.cpp" "$FW/src/Deck.cpp" "$HERE/writer_driver.cpp" \
+    -o "$HERE/_ref/ref_writer.tmp"
+mv "$HERE/_ref/ref_writer.tmp" "$HERE/_ref/ref_writer"
+echo "build_ref: $HERE/_ref/ref_writer"

@@ -49,12 +49,18 @@ def build_oracle() -> str:
 
 
 def build_reference(ref_root: str | None = None) -> str | None:
-    """Compile the reference's own CPU path if its sources are present."""
-    root = ref_root or os.environ.get("NGRAV_REFERENCE", "/root/reference")
-    if not os.path.isfile(os.path.join(root, "projects", "nbody_core", "src", "Tree.cpp")):
+    """Compile the reference's own CPU path if its sources are present.
+
+    ref_root, else $NGRAV_REFERENCE, else the location build_ref.sh knows; the
+    recipe exits 3 when the sources are absent (e.g. on a machine that only
+    runs the prebuilt files), and then this returns None."""
+    root = ref_root or os.environ.get("NGRAV_REFERENCE")
+    cmd = ["bash", os.path.join(HERE, "build_ref.sh")] + ([root] if root else [])
+    r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+    if r.returncode == 3:
         return None
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), root], check=True,
-                   stdout=subprocess.DEVNULL)
+    if r.returncode != 0:
+        raise RuntimeError("build_ref.sh failed:\n" + r.stderr)
     return REF_SO
 
 

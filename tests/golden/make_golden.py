@@ -3,8 +3,9 @@
 Runs the reference's own CPU Barnes-Hut path (projects/nbody_core, compiled
 from its sources by oracle/build_ref.sh into oracle/_ref/libngrav_ref.so) on
 seeded inputs and stores inputs + outputs as compressed .npz files.  Needs
-the reference sources (NGRAV_REFERENCE or /root/reference); the fixtures it
-writes are committed so that tests never need the reference at run time.
+that library (oracle/build_ref.sh builds it where the reference's sources
+are present); the fixtures it writes are committed so that tests never need
+the reference at run time.
 
 All positions and masses are rounded to FP32 before the reference sees them,
 so the GPU state (FP32 / double-float) holds exactly the same inputs.
@@ -13,6 +14,7 @@ so the GPU state (FP32 / double-float) holds exactly the same inputs.
     python tests/golden/make_golden.py scenarios    # scenarios.npz only
     python tests/golden/make_golden.py spline       # spline4k.npz only
     python tests/golden/make_golden.py pp           # pp4k.npz only
+    python tests/golden/make_golden.py writer       # writer_run.npz only
 """
 from __future__ import annotations
 
@@ -119,12 +121,35 @@ def make_block(R, ic):
     np.savez_compressed(os.path.join(HERE, "block4k.npz"), **out)
 
 
+def make_writer():
+    """writer_run.npz: every file of the reference's own run-directory writer
+    (fw::OutputWriter, driven through oracle/writer_driver.cpp's fixed
+    three-frame run), keyed by its path in the run directory with '/' as
+    '__', as raw bytes."""
+    import subprocess
+    import tempfile
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_writer")
+    with tempfile.TemporaryDirectory() as tmp:
+        run = os.path.join(tmp, "run")
+        subprocess.run([exe, run], check=True)
+        out = {}
+        for dirpath, _, files in os.walk(run):
+            for f in files:
+                rel = os.path.relpath(os.path.join(dirpath, f), run)
+                with open(os.path.join(dirpath, f), "rb") as fh:
+                    out[rel.replace(os.sep, "__")] = np.frombuffer(fh.read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "writer_run.npz"), **out)
+
+
 def main():
     orc = ge.load_oracle()
     if orc.build_reference() is None:
         raise SystemExit("reference sources not found; set NGRAV_REFERENCE")
     R = orc.Reference()
     pkg_ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
+    if sys.argv[1:] == ["writer"]:
+        make_writer()
+        return
     if sys.argv[1:] == ["spline"]:
         make_spline(R, pkg_ic)
         return
@@ -140,6 +165,7 @@ def main():
     make_spline(R, pkg_ic)
     make_pp(R, pkg_ic)
     make_block(R, pkg_ic)
+    make_writer()
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
 
     # 1) Plummer N=16,384, seed 0: leaf capacity 16, theta 0.5, eps 0.01, dt 1e-3, 10 KDK steps.

@@ -11,7 +11,11 @@ Pins:
   against fixtures the reference's own generator wrote (tests/golden/
   scenarios.npz, from Scenarios.cpp:355-384 and ic/Plummer.hpp:26-112);
 - the ic_file reader (Scenarios.cpp:292-329) round-trips the writer's format
-  (main.cpp:253-280).
+  (main.cpp:253-280);
+- the run-directory writer (deck.toml, frames/*.npy, diagnostics.csv,
+  manifest.json) byte for byte against the reference's own OutputWriter on a
+  fixed three-frame run (tests/golden/writer_run.npz, written by
+  oracle/writer_driver.cpp linked to framework/src/OutputWriter.cpp).
 """
 import json
 import os
@@ -133,3 +137,31 @@ def test_ic_file_errors(exe, tmp_path):
         deck.write_text(f'[scenario]\ntype = "ic_file"\nic_file = "{path}"\n')
         r = run(exe, "--deck", str(deck), "--dump-ic", str(tmp_path / "o.bin"), check=False)
         assert r.returncode == 1 and what in r.stderr
+
+
+def test_run_directory_bytes_match_reference_writer(tmp_path):
+    """The same driver (oracle/writer_driver.cpp) compiled against this
+    project's writer must write every file of the reference writer's run
+    directory with identical bytes, and no other file."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    host = os.path.join(root, "opengl-physics_gb300", "host")
+    drv = tmp_path / "writer_driver"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", host, os.path.join(root, "oracle", "writer_driver.cpp"),
+                    os.path.join(host, "output_writer.cpp"), os.path.join(host, "deck.cpp"), "-o", str(drv)],
+                   check=True, capture_output=True, timeout=300)
+    run_dir = tmp_path / "run"
+    subprocess.run([str(drv), str(run_dir)], check=True, capture_output=True, timeout=60)
+    got = {}
+    for dirpath, _, files in os.walk(run_dir):
+        for f in files:
+            rel = os.path.relpath(os.path.join(dirpath, f), run_dir).replace(os.sep, "__")
+            with open(os.path.join(dirpath, f), "rb") as fh:
+                got[rel] = fh.read()
+    want = {k: bytes(v) for k, v in load_golden("writer_run.npz").items()}
+    assert sorted(got) == sorted(want)
+    for k in sorted(want):
+        assert got[k] == want[k], f"{k} differs"
+    # and NumPy reads what was written
+    pos = np.load(run_dir / "frames" / "pos_0002.npy")
+    assert pos.dtype == np.float32 and pos.shape == (5, 3)
+    assert np.load(run_dir / "frames" / "ids_0001.npy").shape == (7,)
