@@ -35,3 +35,6 @@ g++ -std=gnu++20 -O2 -DNGRAV_WRITER_REF \
     -o "$HERE/_ref/ref_writer.tmp"
 mv "$HERE/_ref/ref_writer.tmp" "$HERE/_ref/ref_writer"
 echo "build_ref: $HERE/_ref/ref_writer"
+# Where the reference's headers are, for the CPU test that compiles the
+# INTEGRATION.md binding against them (tests/test_binding.py).
+echo "$REF" > "$HERE/_ref/REF_ROOT"
