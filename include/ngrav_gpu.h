@@ -92,7 +92,7 @@ typedef struct ngrav_gpu_diag {
     double com[3];         /* centre of mass */
     double L[3];           /* angular momentum about the COM */
     double P[3];           /* linear momentum */
-    int potential_exact;   /* 1 if the potential is the exact pairwise sum */
+    int potential_exact;   /* 1: exact pairwise sum in FP64; 2: exact pair set, FP32 pair terms; 0: none (NaN) */
 } ngrav_gpu_diag;
 
 typedef struct ngrav_gpu_ferr {
@@ -233,8 +233,13 @@ int ngrav_gpu_get_state(ngrav_gpu_ctx* ctx, double* x, double* y, double* z, dou
 int ngrav_gpu_get_accel(ngrav_gpu_ctx* ctx, double* ax, double* ay, double* az);
 
 /* FP64 conservation diagnostics of the current state.  exact_potential:
- * 1 = exact O(N^2) pairwise potential on the GPU, 0 = let the library choose
- * (exact up to 262,144 particles). */
+ * 1 = exact O(N^2) pairwise potential on the GPU, every pair term in FP64;
+ * 2 = the same pair set with FP32 pair terms and FP64 sums (the offset of a
+ *     pair formed from the double-float positions, so its error is of order
+ *     2^-24 of the separation; Plummer softening, a spline run takes mode 1),
+ *     about 2.5 s at n = 4,194,304 where mode 1 takes minutes;
+ * 0 = mode 1 up to 262,144 particles, else no potential (NaN).
+ * out->potential_exact reports the mode used (0, 1 or 2). */
 int ngrav_gpu_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_diag* out);
 
 /* rms / max / median relative error of the current accelerations against a
@@ -280,6 +285,17 @@ int ngrav_gpu_probe_fp32_peak(int device, double* tflops);
 int ngrav_gpu_diagnostics_noalloc(int device, int64_t n, const float* x, const float* y, const float* z,
                                   const float* vx, const float* vy, const float* vz, const float* m, double G,
                                   double eps, int with_potential, ngrav_gpu_diag* out);
+
+/* Testing support for the capacity-recovery paths (no reference
+ * counterpart; the reference's GPU path fails silently when its pools run
+ * out, src/gpu/GpuBarnesHut.cpp:259-260, :428).  Replaces each pool whose
+ * size is > 0 by one of exactly that size: node records, far and near
+ * interaction-list chunks (128 entries each), and the learned walk's
+ * deferred-pair chunks (the size its pools start at from then on).  The
+ * next evaluation then overflows, detects it on the device, grows the pool
+ * and re-runs; results equal those of a context that never shrank. */
+int ngrav_gpu_debug_shrink_pools(ngrav_gpu_ctx* ctx, int node_cap, int far_chunks, int near_chunks,
+                                 int pend_chunks);
 
 /* Export the last tree for bit-exact checks.  Call with node arrays NULL to
  * get *nnodes; then call again with arrays of that size.

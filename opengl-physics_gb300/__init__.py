@@ -43,7 +43,8 @@ EXPORTS = (
     "ngrav_gpu_block_step", "ngrav_gpu_get_rungs", "ngrav_gpu_adaptive_dt",
     "ngrav_gpu_get_frame_f32",
     "ngrav_gpu_prime", "ngrav_gpu_step", "ngrav_gpu_get_state", "ngrav_gpu_get_accel", "ngrav_gpu_diagnostics",
-    "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_reset_cumulative",
+    "ngrav_gpu_force_error", "ngrav_gpu_get_stats", "ngrav_gpu_debug_tree", "ngrav_gpu_debug_shrink_pools",
+    "ngrav_gpu_reset_cumulative",
     "ngrav_gpu_probe_fp32_peak", "ngrav_gpu_diagnostics_noalloc",
     "ngrav_gpu_set_ensemble", "ngrav_gpu_ensemble_force_error", "ngrav_gpu_ensemble_diagnostics",
     "ngrav_gpu_default_tune_opts", "ngrav_gpu_autotune", "ngrav_gpu_set_tuning",
@@ -200,6 +201,7 @@ def load_library(path: str | None = None):
     L.ngrav_gpu_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     L.ngrav_gpu_debug_tree.argtypes = [ctypes.c_void_p, _I, _U64, _I, _I, _U64, _I, _I, _D, _D, _D, _D, _D, _D]
     L.ngrav_gpu_reset_cumulative.argtypes = [ctypes.c_void_p]
+    L.ngrav_gpu_debug_shrink_pools.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4
     L.ngrav_gpu_probe_fp32_peak.argtypes = [ctypes.c_int, _D]
     L.ngrav_gpu_diagnostics_noalloc.argtypes = [ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 7 + \
         [ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Diag)]
@@ -240,7 +242,7 @@ def diagnostics_noalloc(device, n, x, y, z, vx, vy, vz, m, G, eps, with_potentia
     if rc != OK:
         raise NgravError(rc, "ngrav_gpu_diagnostics_noalloc failed")
     return dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
-                P=list(d.P), potential_exact=bool(d.potential_exact))
+                P=list(d.P), potential_exact=int(d.potential_exact))
 
 
 def probe_fp32_peak(device: int = 0) -> float:
@@ -408,7 +410,7 @@ class NBodySystem:
         d = Diag()
         self._check(self.L.ngrav_gpu_diagnostics(self.h, int(exact_potential), ctypes.byref(d)), self.h)
         return dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
-                    P=list(d.P), potential_exact=bool(d.potential_exact))
+                    P=list(d.P), potential_exact=int(d.potential_exact))
 
     def force_error(self, nsample=4096, seed=12345, fp64_pairs=False):
         f = Ferr()
@@ -423,6 +425,12 @@ class NBodySystem:
 
     def reset_cumulative(self):
         self._check(self.L.ngrav_gpu_reset_cumulative(self.h), self.h)
+
+    def debug_shrink_pools(self, node_cap=0, far_chunks=0, near_chunks=0, pend_chunks=0):
+        """Testing: replace each pool given (> 0) by one of exactly that size,
+        so the next evaluation must detect the overflow, grow and re-run."""
+        self._check(self.L.ngrav_gpu_debug_shrink_pools(self.h, int(node_cap), int(far_chunks), int(near_chunks),
+                                                        int(pend_chunks)), self.h)
 
     def debug_tree(self):
         nn = ctypes.c_int()
@@ -481,7 +489,7 @@ class NBodySystem:
         arr = (Diag * k)()
         self._check(self.L.ngrav_gpu_ensemble_diagnostics(self.h, int(exact_potential), arr), self.h)
         return [dict(kinetic=d.kinetic, potential=d.potential, energy=d.energy, com=list(d.com), L=list(d.L),
-                     P=list(d.P), potential_exact=bool(d.potential_exact)) for d in arr]
+                     P=list(d.P), potential_exact=int(d.potential_exact)) for d in arr]
 
     # ---- learned opening test ----
     def lmac_set_opts(self, **kw):

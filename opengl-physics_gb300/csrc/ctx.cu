@@ -914,9 +914,24 @@ int ngrav_gpu_diagnostics(ngrav_gpu_ctx* ctx, int exact_potential, ngrav_gpu_dia
         out->L[k] = L[k];
         out->P[k] = s1[5 + k];
     }
-    const bool exact = exact_potential || n <= 262144;
-    out->potential_exact = exact ? 1 : 0;
-    if (exact) {
+    if (exact_potential < 0 || exact_potential > 2)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "exact_potential must be 0, 1 or 2");
+    // mode 2: the exact pair set with FP32 pair terms (Plummer; a spline run
+    // takes the FP64 path)
+    const bool pairs32 = exact_potential == 2 && ctx->soft != kSoftSpline;
+    const bool exact = exact_potential != 0 || n <= 262144;
+    out->potential_exact = pairs32 ? 2 : (exact ? 1 : 0);
+    if (pairs32) {
+        const int pb = potential_f32_blocks(n, ctx->sm_count);
+        NG_TRY(ensure_partial(ctx, pb));
+        std::vector<double> hp(pb);
+        launch_potential_f32(n, ctx->P, split, ctx->opts.eps * ctx->opts.eps, pb, ctx->dpartial, ctx->stream);
+        NG_CUDA(cudaMemcpyAsync(hp.data(), ctx->dpartial, sizeof(double) * pb, cudaMemcpyDeviceToHost, ctx->stream));
+        NG_CUDA(cudaStreamSynchronize(ctx->stream));
+        double pot = 0.0;
+        for (int b = 0; b < pb; ++b) pot += hp[b];
+        out->potential = ctx->opts.G * pot;
+    } else if (exact) {
         launch_potential(n, ctx->P, split, ctx->opts.eps * ctx->opts.eps, spline_h(ctx), ctx->dpartial, ctx->stream);
         NG_CUDA(cudaMemcpyAsync(h.data(), ctx->dpartial, sizeof(double) * npb, cudaMemcpyDeviceToHost,
                                 ctx->stream));
@@ -1067,6 +1082,29 @@ int ngrav_gpu_probe_fp32_peak(int device, double* tflops) {
     *tflops = run_fma_probe(sms, s);
     cudaStreamDestroy(s);
     return *tflops > 0.0 ? NGRAV_OK : NGRAV_ERR_CUDA;
+}
+
+int ngrav_gpu_debug_shrink_pools(ngrav_gpu_ctx* ctx, int node_cap, int far_chunks, int near_chunks,
+                                 int pend_chunks) {
+    if (!ctx) return NGRAV_ERR_INVALID_ARG;
+    if (node_cap < 0 || far_chunks < 0 || near_chunks < 0 || pend_chunks < 0)
+        return fail(ctx, NGRAV_ERR_INVALID_ARG, "negative pool size");
+    NG_CUDA(cudaSetDevice(ctx->opts.device));
+    NG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (node_cap > 0) NG_TRY(alloc_nodes(ctx, std::max(node_cap, 1)));
+    if (far_chunks > 0 || near_chunks > 0) {
+        ListBuffers& L = ctx->LB;
+        const long long fc = far_chunks > 0 ? far_chunks : L.far_chunk_cap;
+        const long long nc = near_chunks > 0 ? near_chunks : L.near_chunk_cap;
+        dfree(L.far);
+        dfree(L.far_next);
+        dfree(L.near);
+        dfree(L.near_next);
+        L.far_chunk_cap = L.near_chunk_cap = 0;
+        NG_TRY(alloc_lists(ctx, fc, nc));
+    }
+    if (pend_chunks > 0) NG_TRY(lmac_debug_shrink(ctx, pend_chunks));
+    return NGRAV_OK;
 }
 
 int ngrav_gpu_debug_tree(ngrav_gpu_ctx* ctx, int* nnodes, uint64_t* keys, int* order, int* level, uint64_t* prefix,

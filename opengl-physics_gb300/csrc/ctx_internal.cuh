@@ -140,6 +140,8 @@ void lmac_key(const ngrav_gpu_ctx* ctx, std::vector<unsigned char>& key);
 void lmac_launch_walk(ngrav_gpu_ctx* ctx, const ngrav::WalkParams& wp, const void* model);
 // The deferred-pair pools overflowed: size them to what the walk counted.
 int lmac_grow_pools(ngrav_gpu_ctx* ctx);
+// Testing: free the deferred-pair pools; later walks start them at `chunks`.
+int lmac_debug_shrink(ngrav_gpu_ctx* ctx, long long chunks);
 // After a force evaluation: run the periodic FP64 check, revert on a breach.
 int lmac_after_eval(ngrav_gpu_ctx* ctx);
 void lmac_fill_stats(const ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out);

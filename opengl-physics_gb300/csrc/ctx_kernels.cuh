@@ -23,6 +23,10 @@ void launch_diag_pass1(long long n, const Particles& P, bool split, double* part
 void launch_diag_pass2(long long n, const Particles& P, bool split, double cx, double cy, double cz, double* partial,
                        cudaStream_t s);
 int potential_blocks(long long n);
+// Exact pair potential with FP32 pair terms and FP64 sums (Plummer).
+int potential_f32_blocks(long long n, int sm_count);
+void launch_potential_f32(long long n, const Particles& P, bool split, double eps2, int blocks, double* partial,
+                          cudaStream_t s);
 void launch_potential(long long n, const Particles& P, bool split, double eps2, double spline_h, double* partial,
                       cudaStream_t s);
 int sampler_shares(long long n, int nslots, int sm_count);

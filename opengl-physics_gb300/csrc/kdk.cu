@@ -14,6 +14,8 @@
 // fixed order (deterministic); the potential is the exact FP64 pair sum
 // sum_{i<j} -G m_i m_j / sqrt(r^2 + eps^2).
 #include "engine.cuh"
+
+#include <algorithm>
 #include "softening.cuh"
 #include "ctx_kernels.cuh"
 
@@ -461,6 +463,75 @@ __global__ void __launch_bounds__(kPotThreads) potential_kernel(long long n, con
 }
 
 int potential_blocks(long long n) { return (int)((n + kPotThreads - 1) / kPotThreads); }
+
+// The same pair set (every i < j, Plummer) with FP32 pair terms and FP64
+// sums, for sizes where the FP64 pipe is too slow (n = 4M: 8.8e12 pairs).
+// Thread = target i; sources staged through shared memory as double-float
+// positions, each offset formed as (hi_j - hi_i) + (lo_j - lo_i) in FP32 (an
+// error of order 2^-24 of the separation, not of |x|); a tile's FP32
+// partial joins the thread's FP64 sum per tile.  Block b of B takes target
+// tiles b, 2B-1-b, 2B+b, 4B-1-b, ...: a long and a short row of the
+// triangle in turn, so the blocks finish together.
+constexpr int kPot32Threads = 256;
+
+__device__ double pot32_tile(long long n, long long t0, const float4* __restrict__ pos,
+                             const float4* __restrict__ plo, float eps2, float4* sh, float4* sl) {
+    const long long i = t0 + threadIdx.x;
+    float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
+    if (i < n) {
+        th = pos[i];
+        if (plo) tl = plo[i];
+    }
+    double sum = 0.0;
+    for (long long s0 = t0; s0 < n; s0 += kPot32Threads) {
+        const long long j = s0 + threadIdx.x;
+        __syncthreads();
+        sh[threadIdx.x] = j < n ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        sl[threadIdx.x] = (j < n && plo) ? plo[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        if (i >= n) continue;
+        const int kmax = (int)min((long long)kPot32Threads, n - s0);
+        const int k0 = s0 == t0 ? (int)threadIdx.x + 1 : 0;  // j > i
+        float part = 0.f;
+        for (int k = k0; k < kmax; ++k) {
+            const float4 h = sh[k], l = sl[k];
+            const float dx = (h.x - th.x) + (l.x - tl.x);
+            const float dy = (h.y - th.y) + (l.y - tl.y);
+            const float dz = (h.z - th.z) + (l.z - tl.z);
+            part = fmaf(h.w, rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)))), part);
+        }
+        sum += (double)part;
+    }
+    return -(double)th.w * sum;
+}
+
+__global__ void __launch_bounds__(kPot32Threads) potential_f32_kernel(long long n, const float4* __restrict__ pos,
+                                                                      const float4* __restrict__ plo, float eps2,
+                                                                      double* __restrict__ partial) {
+    __shared__ float4 sh[kPot32Threads], sl[kPot32Threads];
+    __shared__ double red[32];
+    const long long ntiles = (n + kPot32Threads - 1) / kPot32Threads;
+    const long long B = gridDim.x, b = blockIdx.x;
+    double local = 0.0;
+    for (long long base = 0; base < ntiles; base += 2 * B) {
+        const long long ta = base + b, tb = base + 2 * B - 1 - b;
+        if (ta < ntiles) local += pot32_tile(n, ta * kPot32Threads, pos, plo, eps2, sh, sl);
+        if (tb < ntiles) local += pot32_tile(n, tb * kPot32Threads, pos, plo, eps2, sh, sl);
+    }
+    const double t = block_sum_d(local, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+int potential_f32_blocks(long long n, int sm_count) {
+    const long long ntiles = (n + kPot32Threads - 1) / kPot32Threads;
+    const long long want = 8LL * std::max(sm_count, 1);
+    return (int)std::max<long long>(1, std::min(ntiles, want));
+}
+
+void launch_potential_f32(long long n, const Particles& P, bool split, double eps2, int blocks, double* partial,
+                          cudaStream_t s) {
+    potential_f32_kernel<<<blocks, kPot32Threads, 0, s>>>(n, P.pos, split ? P.plo : nullptr, (float)eps2, partial);
+}
 
 void launch_potential(long long n, const Particles& P, bool split, double eps2, double spline_h, double* partial,
                       cudaStream_t s) {

@@ -55,6 +55,7 @@ struct LmacState {
     bool reverted = false;
     int checks = 0;
     double last_check_rms = -1.0;
+    long long start_chunks = 0;  // > 0: deferred-pair pools start at this many chunks (testing)
 };
 
 namespace {
@@ -306,7 +307,7 @@ bool lmac_prepare(ngrav_gpu_ctx* ctx) {
         // every group may park once per round; pools start at 32 deferred
         // pairs per particle (grown to what a round needs if that is short)
         const long long groups = std::max<long long>(ctx->cap_n, 1);
-        const long long est = ctx->n + 1024;
+        const long long est = L->start_chunks > 0 ? L->start_chunks : ctx->n + 1024;
         if (ensure_rounds(ctx, groups, std::max<long long>(L->R.pend_chunk_cap, est)) != NGRAV_OK) use = false;
         L->R.rounds = std::max(2, std::min(kLmMaxRounds, L->opts.rounds));
     }
@@ -359,6 +360,15 @@ void lmac_launch_walk(ngrav_gpu_ctx* ctx, const WalkParams& wp, const void* mode
             launch_lmac_infer(ctx->T, ctx->C, wp, L.R, r, static_cast<const LmacDev*>(model), ctx->sm_count, s);
     }
     ctx->launches += 2 * L.R.rounds - 2;  // beyond the one walk launch counted by the caller
+}
+
+int lmac_debug_shrink(ngrav_gpu_ctx* ctx, long long chunks) {
+    NG_TRY(ensure_state(ctx));
+    LmacState& L = *ctx->lm;
+    // drop the pools (and group state) so the next prepared walk starts at `chunks`
+    free_rounds(L);
+    L.start_chunks = chunks;
+    return NGRAV_OK;
 }
 
 int lmac_grow_pools(ngrav_gpu_ctx* ctx) {

@@ -116,6 +116,29 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
         if (!split) continue;
         if (base + nch > T.cap) {
             if (d == 0) atomicOr(&C->status, kStNodeOverflow);
+            // The slots of this allocation that still fall inside the pool
+            // become inert records (no particles, no children), so the passes
+            // that scan every node up to the pool's end never read an
+            // unwritten record; the parent stays a leaf.  The walk and the
+            // evaluation do not run on the truncated tree, and the host grows
+            // the pool and builds again.
+            if (has) {
+                const int c = base + __popc(hm & ((1u << d) - 1u));
+                if (c < T.cap) {
+                    T.start[c] = 0;
+                    T.count[c] = 0;
+                    T.first_child[c] = -1;
+                    T.parent[c] = node;
+                    T.visit[c] = 0;
+                    T.nchild[c] = 0;
+                    T.level[c] = (unsigned char)(l + 1);
+                    T.cx[c] = T.cx[node];
+                    T.cy[c] = T.cy[node];
+                    T.cz[c] = T.cz[node];
+                    T.half[c] = 0.0;
+                    T.sysroot[c] = T.sysroot[node];
+                }
+            }
             continue;
         }
         if (has) {
@@ -189,12 +212,14 @@ void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* ke
 // Leaf list in key order
 // ---------------------------------------------------------------------------
 
-__global__ void leaf_mark_kernel(NodeArrays T, Counters* C, int* __restrict__ leaf_at,
+__global__ void leaf_mark_kernel(NodeArrays T, Counters* C, long long n, int* __restrict__ leaf_at,
                                  unsigned* __restrict__ flags) {
     const int nn = min(C->next_free, T.cap);
     for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < nn; node += gridDim.x * blockDim.x) {
         if (T.first_child[node] != -1) continue;
         const int s = T.start[node];
+        // inert records of an overflowed allocation own no particles
+        if (T.count[node] <= 0 || s < 0 || s >= n) continue;
         leaf_at[s] = node;
         flags[s] = 1u;
         atomicMax(&C->max_leaf_count, T.count[node]);
@@ -215,7 +240,7 @@ void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, uns
     cudaMemsetAsync(flags, 0, sizeof(unsigned) * n, s);
     long long b1 = ((long long)T.cap + 255) / 256;
     if (b1 > 152 * 8) b1 = 152 * 8;
-    leaf_mark_kernel<<<(unsigned)b1, 256, 0, s>>>(T, C, leaf_at, flags);
+    leaf_mark_kernel<<<(unsigned)b1, 256, 0, s>>>(T, C, n, leaf_at, flags);
     device_exclusive_scan(flags, scan_out, n, sb.scan_tmp, s);
     long long b2 = (n + 255) / 256;
     if (b2 > 152 * 8) b2 = 152 * 8;

@@ -597,7 +597,8 @@ static double now_ms(void) {
 }
 
 int or_bh_time_sampled(int n, const double* x, const double* y, const double* z, const double* m, double G,
-                       double eps, double theta, int ncrit, int quad, int group_stride, double* out) {
+                       double eps, double theta, int ncrit, int quad, int group_stride, double* out,
+                       double* acc_out) {
     or_tree t;
     const double t0 = now_ms();
     if (or_tree_build(&t, n, x, y, z, m, ncrit, 40)) {
@@ -679,10 +680,22 @@ int or_bh_time_sampled(int n, const double* x, const double* y, const double* z,
             free(L.near);
             free(L.stack);
         }
-        free(groups);
         cnt.p2p_pairs = pairs;
     }
     const double t3 = now_ms();
+    if (acc_out) {  /* 3 x n: the sampled targets' accelerations, NaN elsewhere */
+        for (int i = 0; i < n; ++i) acc_out[i] = acc_out[n + i] = acc_out[2 * (size_t)n + i] = NAN;
+        for (int gi = 0; gi < ng; ++gi) {
+            const int g = groups[gi];
+            for (int k = t.first[g]; k < t.first[g] + t.count[g]; ++k) {
+                const int i = t.order[k];
+                acc_out[i] = ax[i];
+                acc_out[n + i] = ay[i];
+                acc_out[2 * (size_t)n + i] = az[i];
+            }
+        }
+    }
+    free(groups);
     free(ax);
     free(ay);
     free(az);

@@ -129,9 +129,11 @@ void or_tree_destroy(void* h);
 /* Bounded-time CPU baseline: full tree build (+ quadrupoles) and the grouped
  * walk over every group_stride-th leaf group only.  out[0] build ms, out[1]
  * walk ms, out[2] fraction of particles walked, out[3] P2P pairs walked.
- * A full step's time extrapolates as out[0] + out[1] / out[2]. */
+ * A full step's time extrapolates as out[0] + out[1] / out[2].  acc_out
+ * (3 x n, or NULL): ax, ay, az of the walked targets, NaN for the others. */
 int or_bh_time_sampled(int n, const double* x, const double* y, const double* z, const double* m, double G,
-                       double eps, double theta, int ncrit, int quad, int group_stride, double* out);
+                       double eps, double theta, int ncrit, int quad, int group_stride, double* out,
+                       double* acc_out);
 
 /* Number of OpenMP threads the oracle will use. */
 int or_num_threads(void);

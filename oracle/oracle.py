@@ -146,16 +146,23 @@ class Oracle(_Common):
     def num_threads(self) -> int:
         return int(self.lib.or_num_threads())
 
-    def time_sampled(self, x, y, z, m, G, eps, theta, ncrit, group_stride, quad=True):
-        """(build_ms, walk_ms, fraction_walked, pairs) of a sampled grouped walk on a full tree."""
+    def time_sampled(self, x, y, z, m, G, eps, theta, ncrit, group_stride, quad=True, with_acc=False):
+        """(build_ms, walk_ms, fraction_walked, pairs) of a sampled grouped walk on a full tree;
+        with_acc: also (ax, ay, az) of the walked targets (NaN for the others)."""
         x, y, z, m = map(_f64, (x, y, z, m))
         out = np.zeros(4)
+        acc = np.empty(3 * len(x)) if with_acc else None
         fn = self.lib.or_bh_time_sampled
         fn.argtypes = [ctypes.c_int, _D, _D, _D, _D, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _D]
-        if fn(len(x), _dp(x), _dp(y), _dp(z), _dp(m), G, eps, theta, ncrit, int(quad), int(group_stride), _dp(out)):
+                       ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+        if fn(len(x), _dp(x), _dp(y), _dp(z), _dp(m), G, eps, theta, ncrit, int(quad), int(group_stride), _dp(out),
+              _dp(acc) if with_acc else None):
             raise RuntimeError("or_bh_time_sampled failed")
-        return float(out[0]), float(out[1]), float(out[2]), float(out[3])
+        res = (float(out[0]), float(out[1]), float(out[2]), float(out[3]))
+        if with_acc:
+            n = len(x)
+            return res + ((acc[:n], acc[n:2 * n], acc[2 * n:]),)
+        return res
 
     def _tree_create(self, n, x, y, z, m, ncrit, max_depth, nn):
         return self.lib.or_tree_create(n, _dp(x), _dp(y), _dp(z), _dp(m), ncrit, max_depth, 1, nn)

@@ -150,3 +150,26 @@ def test_medium_plummer_vs_oracle(pkg, oracle, ic, n, ncrit):
     e = rel_err(ax, ay, az, rx, ry, rz)
     assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (np.median(e), e.max())
     assert st["p2p_pairs"] == cnt["p2p_pairs"] and st["p2c_terms"] == cnt["p2c_terms"]
+
+
+# The bench's own distribution: the two-component galaxy (Hernquist cusp plus
+# a thin exponential disk, eps 0.002), where borderline opening tests and deep
+# leaves are most frequent, at the leaf capacities the bench runs (32, 48)
+# and theta 0.6: the grouped walk of src/Solvers.cpp:279-355.
+@pytest.mark.parametrize("ncrit", [32, 48])
+def test_galaxy_vs_oracle(pkg, oracle, ic, ncrit):
+    n_halo, n_disk = 235930, 26214  # 262,144 bodies in the bench's 9:1 halo/disk ratio
+    x, y, z, vx, vy, vz, m = (a.astype(np.float64) for a in ic.galaxy(n_halo=n_halo, n_disk=n_disk, seed=8))
+    eps, theta = 0.002, 0.6
+    rx, ry, rz, cnt = oracle.bh_accel(x, y, z, m, 1.0, eps, theta, ncrit, counters=True)
+    with make_sim(pkg, 1.0, eps, theta, ncrit) as sim:
+        sim.set_particles(x, y, z, vx, vy, vz, m)
+        ax, ay, az = sim.compute_accel()
+        st = sim.stats()
+        t = sim.debug_tree()
+    ot = oracle.tree(x, y, z, m, ncrit)
+    assert np.array_equal(t["order"], ot["order"])
+    assert st["depth_limited_leaves"] == 0
+    e = rel_err(ax, ay, az, rx, ry, rz)
+    assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (np.median(e), e.max())
+    assert st["p2p_pairs"] == cnt["p2p_pairs"] and st["p2c_terms"] == cnt["p2c_terms"]
