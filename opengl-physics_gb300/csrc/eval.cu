@@ -10,22 +10,29 @@
 // zero for eps > 0 and masked for eps == 0).
 //
 // GB300 mapping.  One warp per group (dynamic scheduling), lane = (target t,
-// slice s): nt targets x floor(32/nt) source slices, slices summed at the end
-// of the group.  A group's targets run in blocks of up to 64, each in one or
-// two passes over every staged chunk (split to keep the lanes busy: 20
-// targets as 4 x 8 + 16 x 2 slices), the second pass's sums parked in shared
-// memory; 80 registers and 8.75 KiB of shared memory per warp keep 6 CTAs
-// of 4 warps per SM.  Far records are staged 32 at a time into shared memory in
-// the group's frame, the next batch loading into registers while this one is
-// evaluated.  Near leaves are staged by TMA bulk copies (cp.async.bulk, one
-// per leaf, completing on an mbarrier with a bounded wait) into a 5 KiB
-// shared-memory buffer, each batch as many leaves (up to 32) as fit by
-// their actual counts; the next batch's leaf records load while a batch is
-// in flight.  (A second buffer would overlap copy and compute within the
-// warp, but halves the resident warps; measured slower.)  In SPLIT precision
-// the staged sources then move from their leaves' frames into the group's,
-// one lane per source, and each lane's partial sums are Kahan compensated
-// once per staged chunk.
+// slice s): nt targets x floor(32/nt) source slices, each slice a contiguous
+// run of the staged sources (odd length, so the slices of a quarter-warp
+// read distinct bank groups), walked four at a time; slices are summed at
+// the end of the group.  A group's targets run in blocks of up to 64, each
+// in one or two passes over every staged chunk (split to keep the lanes
+// busy: 20 targets as 4 x 8 + 16 x 2 slices), the second pass's sums parked
+// in shared memory; 80 registers and about 9 KiB of shared memory per warp
+// keep 6 CTAs of 4 warps per SM.
+// Far records are staged 32 at a time into shared memory in the group's
+// frame; the records of the next batch and the node ids of the one after
+// are loaded while a batch is evaluated, so no batch waits on a list-id ->
+// record load chain.  Near leaves are staged by TMA bulk copies
+// (cp.async.bulk completing on an mbarrier with a bounded wait), one copy
+// per run of leaves whose particles are contiguous (leaves are in key order,
+// so siblings met together form one run), into a 5 KiB shared-memory
+// buffer, each batch as many leaves (up to 32) as fit by their actual
+// counts; the first near batch is in flight during the far field, and each
+// next batch's leaf records load while a batch is evaluated.  (A second
+// buffer would overlap copy and compute within the warp, but halves the
+// resident warps; measured slower.)  In SPLIT precision the staged sources
+// then move from their leaves' frames into the group's (each slot knows its
+// leaf from a byte map written at staging), and each lane's partial sums
+// are Kahan compensated once per staged chunk.
 #include "engine.cuh"
 #include "softening.cuh"
 
@@ -50,6 +57,7 @@ struct __align__(128) EvalSmem {
     int start[kBuffers][32];
     int pre[kBuffers][33];
     unsigned long long bar[2];
+    unsigned char owner[kSrcCap];             // staged slot -> its leaf's lane in the batch (SPLIT)
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -101,9 +109,10 @@ __device__ __forceinline__ int excl_scan(int v, int lane, int& total) {
 }
 
 // Lane mapping for a block of nt <= 32 targets: lane = (target t, slice s),
-// t = lane % nt, s = lane / nt, S = floor(32 / nt) slices; slice s handles
-// sources s, s + S, s + 2S, ...  All lanes of a slice read the same source
-// (shared-memory broadcast); consecutive slices read consecutive sources.
+// t = lane % nt, s = lane / nt, S = floor(32 / nt) slices.  All lanes of a
+// slice read the same source (shared-memory broadcast).  P2P slices are
+// contiguous runs of the staged sources (p2p_chunk); P2C slices take records
+// s, s + S, s + 2S, ... of a 32-record batch.
 struct Lane {
     float tx, ty, tz;
     int sl, S, nt;
@@ -223,56 +232,46 @@ __device__ __forceinline__ void for_passes(Lane& g, bool two, EvalSmem& sm, int 
 }
 
 // SOFT: 0 Plummer, 1 Plummer with eps = 0 (the self pair gives 0), 2 spline.
+template <int SOFT>
+__device__ __forceinline__ void p2p_pair(const float4& a, float tx, float ty, float tz, float eps2, float ih,
+                                         float& px, float& py, float& pz) {
+    const float dx = a.x - tx, dy = a.y - ty, dz = a.z - tz;
+    float f;
+    if (SOFT == 2) {
+        f = pair_factor<kSoftSpline>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), a.w, 0.f, ih);
+    } else {
+        const float r = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        const float ir = rsqrtf(r);
+        f = a.w * (ir * ir * ir);
+        if (SOFT == 1) f = r > 0.f ? f : 0.f;
+    }
+    px = fmaf(f, dx, px);
+    py = fmaf(f, dy, py);
+    pz = fmaf(f, dz, pz);
+}
+
+// One staged chunk of ns sources against the lane's target.  Slice s takes a
+// contiguous run of len = ceil(ns / S) sources (rounded up to odd: the S
+// slices of a quarter-warp then read distinct shared-memory bank groups in
+// the same LDS.128), walked four at a time with immediate offsets from one
+// pointer, in two independent accumulation chains.
 template <bool SPLIT, int SOFT>
 __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_src, int ns, float eps2, float ih) {
     if (!g.active) return;
     float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
     const float tx = g.tx, ty = g.ty, tz = g.tz;
-    const int S = g.S;
-    int j = g.sl;
-    for (; j + S < ns; j += 2 * S) {  // two independent chains per lane
-        const float4 a = s_src[j];
-        const float4 b = s_src[j + S];
-        const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
-        const float bx_ = b.x - tx, by_ = b.y - ty, bz_ = b.z - tz;
-        float fa, fb;
-        if (SOFT == 2) {
-            fa = pair_factor<kSoftSpline>(fmaf(ax_, ax_, fmaf(ay_, ay_, az_ * az_)), a.w, 0.f, ih);
-            fb = pair_factor<kSoftSpline>(fmaf(bx_, bx_, fmaf(by_, by_, bz_ * bz_)), b.w, 0.f, ih);
-        } else {
-            const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
-            const float rb = fmaf(bx_, bx_, fmaf(by_, by_, fmaf(bz_, bz_, eps2)));
-            const float ia = rsqrtf(ra), ib = rsqrtf(rb);
-            fa = a.w * (ia * ia * ia);
-            fb = b.w * (ib * ib * ib);
-            if (SOFT == 1) {
-                fa = ra > 0.f ? fa : 0.f;
-                fb = rb > 0.f ? fb : 0.f;
-            }
-        }
-        px = fmaf(fa, ax_, px);
-        py = fmaf(fa, ay_, py);
-        pz = fmaf(fa, az_, pz);
-        qx = fmaf(fb, bx_, qx);
-        qy = fmaf(fb, by_, qy);
-        qz = fmaf(fb, bz_, qz);
+    const int len = ((ns + g.S - 1) / g.S) | 1;
+    const int b = min(ns, g.sl * len);
+    const float4* p = s_src + b;
+    const float4* const pe = s_src + min(ns, b + len);
+    for (; p + 4 <= pe; p += 4) {
+        const float4 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3];
+        p2p_pair<SOFT>(a0, tx, ty, tz, eps2, ih, px, py, pz);
+        p2p_pair<SOFT>(a1, tx, ty, tz, eps2, ih, qx, qy, qz);
+        p2p_pair<SOFT>(a2, tx, ty, tz, eps2, ih, px, py, pz);
+        p2p_pair<SOFT>(a3, tx, ty, tz, eps2, ih, qx, qy, qz);
     }
-    if (j < ns) {
-        const float4 a = s_src[j];
-        const float ax_ = a.x - tx, ay_ = a.y - ty, az_ = a.z - tz;
-        float fa;
-        if (SOFT == 2) {
-            fa = pair_factor<kSoftSpline>(fmaf(ax_, ax_, fmaf(ay_, ay_, az_ * az_)), a.w, 0.f, ih);
-        } else {
-            const float ra = fmaf(ax_, ax_, fmaf(ay_, ay_, fmaf(az_, az_, eps2)));
-            const float ia = rsqrtf(ra);
-            fa = a.w * (ia * ia * ia);
-            if (SOFT == 1) fa = ra > 0.f ? fa : 0.f;
-        }
-        px = fmaf(fa, ax_, px);
-        py = fmaf(fa, ay_, py);
-        pz = fmaf(fa, az_, pz);
-    }
+    for (; p < pe; ++p) p2p_pair<SOFT>(p[0], tx, ty, tz, eps2, ih, px, py, pz);
     accumulate<SPLIT>(g, px + qx, py + qy, pz + qz);
 }
 
@@ -311,105 +310,147 @@ __device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA
     accumulate<SPLIT>(g, px, py, pz);
 }
 
-// One near leaf's info (lane = list entry), loaded into registers.
+// One near leaf's info (lane = list entry), loaded into registers.  The
+// leaf centre's double-float halves are kept as loaded: the frame shift is
+// formed only when the batch is staged, a batch later, so these loads never
+// stall the batch being computed.
 struct NearInfo {
     int start, cnt;
-    float4 shift;
+    float4 h, l;
 };
 
+// Publish a batch's info to buffer `b` and start its TMA copies: one bulk
+// copy per run of leaves whose particles are contiguous in memory (leaves
+// are in key order, so siblings met together form one run), issued by the
+// run's first lane.  In SPLIT precision each lane also forms its leaf's
+// frame shift and marks the staged slots of its leaf in `owner`.  Returns
+// the number of staged sources.
 template <bool SPLIT>
-__device__ __forceinline__ NearInfo load_near_info(const NodeArrays& T, const ListBuffers& LB, int chunk, int idx,
-                                                   bool valid, const float4& gchi, const float4& gclo) {
-    NearInfo r;
-    r.start = 0;
-    r.cnt = 0;
-    r.shift = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (valid) {
-        const int node = LB.near[(long long)chunk * kListChunk + (idx & (kListChunk - 1))];
-        const float4 Cw = T.wC[node];
-        r.start = __float_as_int(Cw.z);
-        r.cnt = __float_as_int(Cw.w) & 0xFFFFFF;
-        if (SPLIT) {
-            const float4 h = T.chi[node], l = T.clo[node];
-            r.shift = make_float4((h.x - gchi.x) + (l.x - gclo.x), (h.y - gchi.y) + (l.y - gclo.y),
-                                  (h.z - gchi.z) + (l.z - gclo.z), 0.f);
-        }
-    }
-    return r;
-}
-
-// Publish a batch's info to buffer `b` and start its TMA copies; returns the
-// number of staged sources.
 __device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& in, int lane,
-                                          const float4* __restrict__ src) {
+                                          const float4* __restrict__ src, const float4& gchi, const float4& gclo) {
     int tot;
     const int ex = excl_scan(in.cnt, lane, tot);
     sm.start[b][lane] = in.start;
     sm.pre[b][lane] = ex;
     if (lane == 31) sm.pre[b][32] = tot;
-    sm.shift[b][lane] = in.shift;
+    if (SPLIT) {
+        sm.shift[b][lane] = make_float4((in.h.x - gchi.x) + (in.l.x - gclo.x), (in.h.y - gchi.y) + (in.l.y - gclo.y),
+                                        (in.h.z - gchi.z) + (in.l.z - gclo.z), 0.f);
+        for (int k = 0; k < in.cnt; ++k) sm.owner[ex + k] = (unsigned char)lane;
+    }
     if (tot > 0) {
+        // run heads: a staged leaf that does not continue the previous lane's range
+        const int pend = __shfl_up_sync(0xffffffffu, in.start + in.cnt, 1);
+        const int pcnt = __shfl_up_sync(0xffffffffu, in.cnt, 1);
+        const bool head = in.cnt > 0 && (lane == 0 || pcnt == 0 || pend != in.start);
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        const unsigned later = heads & ~(0xFFFFFFFFu >> (31 - lane));  // heads after this lane
+        const int nxt = later ? __ffs(later) - 1 : 31;
+        const int ex_next = __shfl_sync(0xffffffffu, ex, nxt);
+        const int run_end = later ? ex_next : tot;
         if (lane == 0) mbar_expect_tx(&sm.bar[b], (unsigned)tot * 16u);
         __syncwarp();
-        if (in.cnt > 0) {
+        if (head) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            tma_load_1d(&sm.src[b][ex], src + in.start, (unsigned)in.cnt * 16u, &sm.bar[b]);
+            tma_load_1d(&sm.src[b][ex], src + in.start, (unsigned)(run_end - ex) * 16u, &sm.bar[b]);
         }
     }
     __syncwarp();
     return tot;
 }
 
-// Info of near-list entries pos .. pos+31 (lane = entry), which may run
-// into the next 128-entry chunk; lanes past the list get count 0.
+// A leaf's staging info from its node id (-1: past the list, count 0).
 template <bool SPLIT>
-__device__ __forceinline__ NearInfo load_near_batch(const NodeArrays& T, const ListBuffers& LB, int chunk, int pos,
-                                                    int lane, int nnear, const float4& gchi, const float4& gclo) {
-    const int e = pos + lane;
-    const bool valid = e < nnear;
-    const bool next = (pos & (kListChunk - 1)) + lane >= kListChunk;
-    int c = chunk;
-    if (valid && next) c = LB.near_next[chunk];
-    return load_near_info<SPLIT>(T, LB, c, e, valid, gchi, gclo);
+__device__ __forceinline__ NearInfo near_info_of(const NodeArrays& T, int node) {
+    NearInfo r;
+    r.start = 0;
+    r.cnt = 0;
+    r.h = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.l = r.h;
+    if (node >= 0) {
+        const float4 Cw = T.wC[node];
+        r.start = __float_as_int(Cw.z);
+        r.cnt = __float_as_int(Cw.w) & 0xFFFFFF;
+        if (SPLIT) {
+            r.h = T.chi[node];
+            r.l = T.clo[node];
+        }
+    }
+    return r;
+}
+
+// The near list's node ids of entries pos .. pos+63 held in registers (w0:
+// pos + lane, w1: pos + 32 + lane; -1 past the list), so a batch's leaf
+// records load from ids that arrived a batch earlier.  A batch takes at most
+// 32 entries, so the ids still needed after it are in the window and only
+// its tail is refilled from memory; the window spans at most two of the
+// list's 128-entry chunks (ca holds pos, cb is the next one).
+struct NearWindow {
+    int pos, w0, w1, ca, cb;
+};
+
+__device__ __forceinline__ int near_entry(const ListBuffers& LB, const NearWindow& W, int e, int nnear) {
+    if (e >= nnear) return -1;
+    const int c = (e >> 7) == (W.pos >> 7) ? W.ca : W.cb;
+    return LB.near[(long long)c * kListChunk + (e & (kListChunk - 1))];
+}
+
+__device__ __forceinline__ NearWindow near_window(const ListBuffers& LB, int first, int nnear, int lane) {
+    NearWindow W;
+    W.pos = 0;
+    W.ca = first;
+    W.cb = nnear > kListChunk ? LB.near_next[first] : -1;
+    W.w0 = lane < nnear ? LB.near[(long long)first * kListChunk + lane] : -1;
+    W.w1 = 32 + lane < nnear ? LB.near[(long long)first * kListChunk + 32 + lane] : -1;
+    return W;
+}
+
+// Move the window forward by nb <= 32 entries.
+__device__ __forceinline__ void near_advance(const ListBuffers& LB, NearWindow& W, int nb, int nnear, int lane) {
+    const int i0 = nb + lane, i1 = nb + 32 + lane;  // old-window indices of the new w0, w1
+    const int a0 = __shfl_sync(0xffffffffu, W.w0, i0 & 31);
+    const int a1 = __shfl_sync(0xffffffffu, W.w1, i0 & 31);
+    const int b1 = __shfl_sync(0xffffffffu, W.w1, i1 & 31);
+    const int n0 = i0 < 32 ? a0 : a1;
+    const int n1 = i1 < 64 ? b1 : near_entry(LB, W, W.pos + i1, nnear);
+    W.w0 = n0;
+    W.w1 = n1;
+    const int np = W.pos + nb;
+    if ((np >> 7) != (W.pos >> 7)) {  // the window now starts in the next chunk
+        W.ca = W.cb;
+        W.cb = ((np >> 7) + 1) * kListChunk < nnear ? LB.near_next[W.ca] : -1;
+    }
+    W.pos = np;
 }
 
 // Stage the longest prefix of the 32 leaves in `in` whose sources fit `cap`
 // (at least one: every leaf fits the buffer outside the big-leaf path).
 // Returns the staged source count; nb = leaves staged.
+template <bool SPLIT>
 __device__ __forceinline__ int stage_fitting(EvalSmem& sm, const NearInfo& in, int lane,
-                                             const float4* __restrict__ src, int cap, int& nb) {
+                                             const float4* __restrict__ src, int cap, int& nb,
+                                             const float4& gchi, const float4& gclo) {
     int tot;
     const int ex = excl_scan(in.cnt, lane, tot);
     const bool fits = ex + in.cnt <= cap || lane == 0;
     nb = __popc(__ballot_sync(0xffffffffu, fits));  // counts are >= 0: a prefix of lanes
     NearInfo mine = in;
     if (lane >= nb) mine.cnt = 0;
-    return stage_batch(sm, 0, mine, lane, src);
+    return stage_batch<SPLIT>(sm, 0, mine, lane, src, gchi, gclo);
 }
 
 // Moves a staged batch of ns sources from their leaves' frames into the
-// group's frame, lane-parallel over sources (lane = slot within a window of
-// 32).  Source j belongs to the last of the nb staged leaves whose first
-// slot is <= j; leaves hold at least one source, so their first slots are
-// distinct and bit i of a window's mask marks a leaf starting at slot
-// base + i.  (Lanes past the near list stage nothing and start at slot ns.)
-__device__ __forceinline__ void shift_batch(EvalSmem& sm, int ns, int nb, int lane) {
-    const int first = lane < nb ? sm.pre[0][lane] : ns;
-    int before = 0;  // leaves starting before the window
-    for (int base = 0; base < ns; base += 32) {
-        const unsigned bit = first >= base && first < base + 32 ? 1u << (first - base) : 0u;
-        const unsigned starts = __reduce_or_sync(0xffffffffu, bit);
-        const int j = base + lane;
-        if (j < ns) {
-            const int leaf = before + __popc(starts & (0xffffffffu >> (31 - lane))) - 1;
-            const float4 sh = sm.shift[0][leaf];
-            float4 v = sm.src[0][j];
-            v.x += sh.x;
-            v.y += sh.y;
-            v.z += sh.z;
-            sm.src[0][j] = v;
-        }
-        before += __popc(starts);
+// group's frame: source j adds the shift of the leaf that owns its slot.
+// The iterations are independent, so their shared-memory loads overlap.
+__device__ __forceinline__ void shift_batch(EvalSmem& sm, int ns, int lane) {
+#pragma unroll 4
+    for (int j = lane; j < ns; j += 32) {
+        const float4 sh = sm.shift[0][sm.owner[j]];
+        float4 v = sm.src[0][j];
+        v.x += sh.x;
+        v.y += sh.y;
+        v.z += sh.z;
+        sm.src[0][j] = v;
     }
 }
 
@@ -491,50 +532,73 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
             const int nblk = min(kBlockTargets, gcount - t0);
             const int b0 = kPassSplit.first[nblk];
             const bool two = b0 < nblk;
+            // Far records come in batches of 32 list entries.  The records of
+            // batch k are loaded during batch k-1 and the node ids of batch
+            // k+1 during batch k-1 as well (chunk links one chunk ahead), so
+            // no batch waits on a list-id -> record load chain of its own.
+            // The first near batch's leaf records load alongside the first
+            // far batch, and its copies are in flight during the far field.
+            int fcur = far_first;                                    // chunk of the next ids to load
+            int fnxt = nfar > kListChunk ? LB.far_next[far_first] : -1;
+            float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, D = A;
+            {
+                const int id0 = lane < nfar ? LB.far[(long long)fcur * kListChunk + lane] : -1;
+                if (id0 >= 0) {
+                    A = T.wA[id0];
+                    D = T.wD[id0];
+                    if (QUAD) B = T.wB[id0];
+                }
+            }
+            int fid = 32 + lane < nfar ? LB.far[(long long)fcur * kListChunk + 32 + lane] : -1;  // batch 1
+            int nb = 0, ns_cur = 0;
+            NearWindow W = {0, -1, -1, -1, -1};
+            NearInfo info;
+            if (!big_leaves) {
+                W = near_window(LB, near_first, nnear, lane);
+                info = near_info_of<SPLIT>(T, W.w0);
+            }
             Lane g = make_lane(src, gstart + t0, b0, lane);
             if (two) save_pass(sm, make_lane(src, gstart + t0 + b0, nblk - b0, lane), lane);
+            if (!big_leaves) {
+                ns_cur = stage_fitting<SPLIT>(sm, info, lane, src, tile, nb, gchi, gclo);
+                near_advance(LB, W, nb, nnear, lane);
+            }
 
-            // ---- far field: batches of 32 records; the next batch loads while this one computes ----
-            {
-                int c = far_first;
-                float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, D = A;
-                if (lane < nfar) {
-                    const int node = LB.far[(long long)c * kListChunk + lane];
-                    A = T.wA[node];
-                    D = T.wD[node];
-                    if (QUAD) B = T.wB[node];
-                }
-                for (int b = 0; b < nfar; b += 32) {
-                    if (b + lane < nfar) {
-                        float4 rA = A;
-                        if (SPLIT) {
-                            rA.x = (A.x - gchi.x) + (D.x - gclo.x);
-                            rA.y = (A.y - gchi.y) + (D.y - gclo.y);
-                            rA.z = (A.z - gchi.z) + (D.z - gclo.z);
-                        }
-                        sm.farA[lane] = rA;
-                        if (QUAD) {
-                            sm.farB[lane] = B;
-                            sm.farQ[lane] = make_float2(D.w, -(B.x + B.y));
-                        }
+            // ---- far field ----
+            for (int b = 0, k = 0; b < nfar; b += 32, ++k) {
+                if (b + lane < nfar) {
+                    float4 rA = A;
+                    if (SPLIT) {
+                        rA.x = (A.x - gchi.x) + (D.x - gclo.x);
+                        rA.y = (A.y - gchi.y) + (D.y - gclo.y);
+                        rA.z = (A.z - gchi.z) + (D.z - gclo.z);
                     }
-                    __syncwarp();
-                    const int nb = b + 32;
-                    if (nb < nfar) {
-                        if ((nb & (kListChunk - 1)) == 0) c = LB.far_next[c];
-                        if (nb + lane < nfar) {
-                            const int node = LB.far[(long long)c * kListChunk + (nb & (kListChunk - 1)) + lane];
-                            A = T.wA[node];
-                            D = T.wD[node];
-                            if (QUAD) B = T.wB[node];
-                        }
+                    sm.farA[lane] = rA;
+                    if (QUAD) {
+                        sm.farB[lane] = B;
+                        sm.farQ[lane] = make_float2(D.w, -(B.x + B.y));
                     }
-                    const int nrec = min(32, nfar - b);
-                    for_passes(g, two, sm, lane, [&](Lane& x) {
-                        p2c_chunk<SPLIT, QUAD, SOFT>(x, sm.farA, sm.farB, sm.farQ, nrec, wp.eps2, wp.ih);
-                    });
-                    __syncwarp();
                 }
+                __syncwarp();
+                if (fid >= 0) {  // records of batch k+1
+                    A = T.wA[fid];
+                    D = T.wD[fid];
+                    if (QUAD) B = T.wB[fid];
+                }
+                fid = -1;
+                const int e2 = b + 64;  // first entry of batch k+2
+                if (e2 < nfar) {
+                    if ((e2 & (kListChunk - 1)) == 0) {  // batch k+2 opens the next chunk
+                        fcur = fnxt;
+                        fnxt = e2 + kListChunk < nfar ? LB.far_next[fcur] : -1;
+                    }
+                    if (e2 + lane < nfar) fid = LB.far[(long long)fcur * kListChunk + (e2 & (kListChunk - 1)) + lane];
+                }
+                const int nrec = min(32, nfar - b);
+                for_passes(g, two, sm, lane, [&](Lane& x) {
+                    p2c_chunk<SPLIT, QUAD, SOFT>(x, sm.farA, sm.farB, sm.farQ, nrec, wp.eps2, wp.ih);
+                });
+                __syncwarp();
             }
             p2c += (unsigned long long)nblk * (unsigned long long)nfar;
 
@@ -542,24 +606,15 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
             // staging buffer, by their actual counts) staged by TMA ----
             int total = 0;
             if (!big_leaves) {
-                int pos = 0;               // list index of the batch's first leaf
-                int chunk = near_first;    // list chunk holding entry `pos`
-                NearInfo info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
-                int nb = 0;
-                int ns_cur = stage_fitting(sm, info, lane, src, tile, nb);
-                pos += nb;
-                if (pos < nnear) {
-                    if ((pos & (kListChunk - 1)) < nb) chunk = LB.near_next[chunk];  // crossed a chunk boundary
-                    info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
-                }
-                int nb_cur = nb;
+                // batch 0 was staged before the far field
+                if (W.pos < nnear) info = near_info_of<SPLIT>(T, W.w0);
                 while (ns_cur > 0) {
                     if (!mbar_wait(&sm.bar[0], phase[0])) {
                         timeout = true;
                         break;
                     }
                     phase[0] ^= 1u;
-                    if (SPLIT) shift_batch(sm, ns_cur, nb_cur, lane);  // into the group's frame
+                    if (SPLIT) shift_batch(sm, ns_cur, lane);  // into the group's frame
                     __syncwarp();
                     for_passes(g, two, sm, lane,
                                [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src[0], ns_cur, wp.eps2, wp.ih); });
@@ -568,14 +623,10 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
                     // stage the next batch (its info is in registers), then fetch
                     // the info of the one after
                     int ns_next = 0;
-                    if (pos < nnear) {
-                        ns_next = stage_fitting(sm, info, lane, src, tile, nb);
-                        nb_cur = nb;
-                        pos += nb;
-                        if (pos < nnear) {
-                            if ((pos & (kListChunk - 1)) < nb) chunk = LB.near_next[chunk];
-                            info = load_near_batch<SPLIT>(T, LB, chunk, pos, lane, nnear, gchi, gclo);
-                        }
+                    if (W.pos < nnear) {
+                        ns_next = stage_fitting<SPLIT>(sm, info, lane, src, tile, nb, gchi, gclo);
+                        near_advance(LB, W, nb, nnear, lane);
+                        if (W.pos < nnear) info = near_info_of<SPLIT>(T, W.w0);
                     }
                     ns_cur = ns_next;
                 }
