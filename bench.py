@@ -24,7 +24,11 @@ value   = N * K / (device time of the learned arm's K timed steps, CUDA
           arm's figure and the ratio are in config.
 e2e     = the same metric through the C-ABI with host buffers: per step
           ngrav_gpu_set_state_f32 from pinned host memory, ngrav_gpu_step(1),
-          ngrav_gpu_get_state into pinned FP64 arrays, wall clock.
+          ngrav_gpu_get_state into pinned FP64 arrays, wall clock (10 steps;
+          the three calls' shares are on the line).
+drift   = energy, momentum and angular-momentum drift of each arm over its
+          timed steps (FP64 diagnostics; the potential is the exact pair sum
+          with FP32 pair terms and FP64 sums).
 roofline: the evaluation kernel (P2P + P2C, FP32 pipe): algorithmic
           flops (20 per P2P pair + 60 per P2C term, device-counted) / its
           event-timed duration, against the measured FP32 FMA peak.
@@ -36,7 +40,13 @@ roofline_sort: the HBM-bound part of the tree build (radix sort + the
           that phase, against the measured copy bandwidth.
 cpu_baseline: the oracle (C restatement of the reference's CPU path) on the
           host cores, bounded sample: full tree build + walk over every
-          k-th leaf group, extrapolated to a full step.
+          k-th leaf group, extrapolated to a full step; its own rms error
+          against the FP64 direct sum is stated.
+configs: compact records of the task's other configurations: C2 (Plummer
+          1M, plain vs split precision, 100 steps, error and drift), C3 (512-
+          system ensemble, autotuned, graph steps) and C5 (16.8M cold
+          collapse, 200 steps, error and key-depth limit every 20 steps);
+          --workload plummer1m / ensemble512 / collapse16m runs each alone.
 With --gpus N > 1 (torchrun), each rank runs an independent replica (the
 path has no data-parallel split on one system); value sums the replicas.
 """
@@ -64,6 +74,8 @@ WORKLOADS = {
     "galaxy1m": ("galaxy", {"n_halo": 943718, "n_disk": 104858}, 0.002, 2e-4, 0.6, 16),
     "plummer1m": ("plummer", {"n": 1048576, "seed": 1}, 0.005, 5e-4, 0.5, 16),
     "plummer16k": ("plummer", {"n": 16384, "seed": 0}, 0.01, 1e-3, 0.5, 16),
+    # cold collapse of a uniform ball, 16.8M, learned test (its own line: collapse_run)
+    "collapse16m": ("uniform_ball", {"n": 16777216, "seed": 4}, 0.001, 1e-4, 0.6, 32),
     # 512 Plummer spheres, N_i log-uniform in [1024, 65536] (~7.9M), one launch per phase
     "ensemble512": ("ensemble", {"nsys": 512}, 0.01, 1e-3, 0.6, 16),
 }
@@ -138,53 +150,169 @@ def make_inputs(pkg_ic, workload):
     return arrs, eps, dt, theta, ncrit
 
 
-def run_ensemble(args, pkg, ic, rank, world, dev):
-    """Ensemble of independent systems: autotuned leaf capacity, one launch per
-    phase for all systems, CUDA-graph steps; per-system error on 256 targets."""
-    gen, kw, eps, dt, theta, ncrit = WORKLOADS[args.workload]
+def ensemble_run(pkg, ic, dev, steps, warmup, tune_reps=2, clocks=None):
+    """C3: 512 independent Plummer spheres (log-uniform N in [1024, 65536],
+    system i seed i, ~7.9M particles), eps 0.01, theta 0.6, dt 1e-3: the
+    leaf capacity autotuned, one launch per phase for all systems, CUDA-graph
+    steps; per-system force error on 256 targets each (FP32 pairs, FP64
+    sums) and per-system energy drift over the timed steps (exact FP64 pair
+    potential of each system)."""
+    gen, kw, eps, dt, theta, ncrit = WORKLOADS["ensemble512"]
     arrs, off = ic.ensemble(**kw)
     n, nsys = len(arrs[0]), len(off) - 1
-    sim = pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=ncrit, device=dev,
-                          timing=True)
-    sim.set_particles_f32(*arrs)
-    sim.set_ensemble(off)
-    sim.prime()
-    tune = sim.autotune(reps=2, check_targets=4096)
-    sim.prime()
-    clocks = ClockSampler(dev)
-    st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks)
-    rms, mx = sim.ensemble_force_error(256, seed=1)
-    value = world * n / (ms_step * 1e-3)
+    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=ncrit, device=dev,
+                         timing=True) as sim:
+        sim.set_particles_f32(*arrs)
+        sim.set_ensemble(off)
+        sim.prime()
+        tune = sim.autotune(reps=tune_reps, check_targets=4096)
+        sim.prime()
+        st, ms_step, clk, (d0, d1) = timed(sim, steps, warmup, dt, clocks,
+                                           diag=lambda: sim.ensemble_diagnostics(exact_potential=True))
+        rms, mx = sim.ensemble_force_error(256, seed=1)
+    dE = np.array([(b["energy"] - a["energy"]) / abs(a["energy"]) for a, b in zip(d0, d1)])
     flops = 20.0 * st["cum_p2p_pairs"] + 60.0 * st["cum_p2c_terms"]
     achieved = flops / (st["cum_ms_force"] * 1e-3) / 1e12 if st["cum_ms_force"] > 0 else None
+    return {"n": n, "systems": nsys, "n_min": int(np.diff(off).min()), "n_max": int(np.diff(off).max()),
+            "eps": eps, "theta": theta, "dt": dt, "steps": steps, "warmup": warmup,
+            "value": n / (ms_step * 1e-3), "ms_per_step": ms_step, "leaf_capacity": tune["leaf_capacity"],
+            "autotune": tune, "graph_replays": st["graph_replays"], "gpu_launches": st["cum_launches"],
+            "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
+            "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
+            "eval_tflops": achieved, "ms_phases_last_eval": phases(st),
+            "per_system_force_err_rms": {"median": float(np.median(rms)), "max": float(rms.max()),
+                                         "targets_per_system": 256},
+            "per_system_force_err_max": float(mx.max()),
+            "per_system_energy_drift": {"median_abs": float(np.median(np.abs(dE))), "max_abs": float(np.abs(dE).max())},
+            "clocks": clk}
+
+
+def run_ensemble(args, pkg, ic, rank, world, dev):
+    """The C3 ensemble as its own bench line."""
+    r = ensemble_run(pkg, ic, dev, args.steps, args.warmup, clocks=ClockSampler(dev))
     peak = pkg.probe_fp32_peak(dev)
     if rank == 0:
         line = {
             "metric": "particle-steps/s, ensemble of 512 Plummer spheres (log-uniform N in [1024, 65536])",
-            "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded Plummer generator, system i seed i)",
-            "config": {"workload": args.workload, "n": n, "systems": nsys, "n_min": int(np.diff(off).min()),
-                       "n_max": int(np.diff(off).max()), "eps": eps, "theta": theta, "dt": dt,
-                       "leaf_capacity": tune["leaf_capacity"], "autotune": tune, "graph_replays": st["graph_replays"],
-                       "p2p_pairs_per_step": st["cum_p2p_pairs"] / max(1, st["cum_evals"]),
-                       "p2c_terms_per_step": st["cum_p2c_terms"] / max(1, st["cum_evals"]),
-                       "ms_phases_last_eval": phases(st),
-                       "per_system_force_err_rms": {"median": float(np.median(rms)), "max": float(rms.max()),
-                                                    "targets_per_system": 256},
-                       "per_system_force_err_max": float(mx.max())},
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+            "value": world * r["value"], "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Plummer generator, system i seed i)",
+            "config": {"workload": "ensemble512", **{k: v for k, v in r.items() if k not in ("clocks", "value")}},
+            "roofline": {"bound": "fp32", "achieved": r["eval_tflops"], "peak": peak, "unit": "TFLOP/s",
+                         "frac": (r["eval_tflops"] / peak) if r["eval_tflops"] and peak else None, "traffic": None,
                          "kernel": "eval_kernel (P2P 20 flops/pair + P2C 60 flops/term)"},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": st["cum_launches"], "clocks": clk,
+            "cpu_baseline": None, "e2e": None, "gpu_launches": r["gpu_launches"], "clocks": r["clocks"],
         }
         print(json.dumps(line), flush=True)
-    sim.close()
     return 0
 
 
+def precision_run(pkg, ic, dev, steps=100):
+    """C2: Plummer N = 1,048,576 (seed 1), eps 0.005, theta 0.5, leaf
+    capacity 16, monopole + quadrupole, KDK dt 5e-4 for `steps` steps, in
+    PLAIN (FP32 absolute positions, plain sums) and SPLIT precision
+    (double-float state, leaf-frame FP32 offsets, Kahan sums; FP64 only in
+    the top moments and the diagnostics).  Each: rms / max / median relative
+    force error against the FP64 direct sum (FP64 pair terms) on 4,096
+    uniformly sampled targets, at the start and after the steps, and the
+    energy, momentum and angular-momentum drift (exact pair potential)."""
+    arrs = ic.plummer(1048576, seed=1)
+    eps, dt, theta = 0.005, 5e-4, 0.5
+    mtot = float(np.sum(arrs[6], dtype=np.float64))
+    out = {"n": 1048576, "eps": eps, "theta": theta, "dt": dt, "leaf_capacity": 16, "steps": steps}
+    for name, prec in (("plain", pkg.PRECISION_PLAIN), ("split", pkg.PRECISION_SPLIT)):
+        with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=theta, dt=dt), leaf_capacity=16, precision=prec,
+                             device=dev, timing=True) as sim:
+            sim.set_particles_f32(*arrs)
+            sim.prime()
+            fe0 = sim.force_error(4096, seed=2024, fp64_pairs=True)
+            d0 = sim.diagnostics(exact_potential=2)
+            sim.reset_cumulative()
+            sim.step(steps, dt)
+            st = sim.stats()
+            d1 = sim.diagnostics(exact_potential=2)
+            fe1 = sim.force_error(4096, seed=2024, fp64_pairs=True)
+        out[name] = {"force_err_start": {k: fe0[k] for k in ("rms", "max", "median")},
+                     "force_err_end": {k: fe1[k] for k in ("rms", "max", "median")},
+                     **drift(d0, d1, mtot), "ms_per_step": st["cum_ms_step"] / steps,
+                     "value": 1048576 / (st["cum_ms_step"] / steps * 1e-3)}
+    return out
+
+
+def collapse_run(pkg, ic, dev, steps=200, every=20, model=None, budget=3.5e-4, energy=False, n=16777216):
+    """C5: cold collapse of a uniform ball, N = 16,777,216 (cube rejection,
+    seed 4), at rest, G = 1, eps 0.001, KDK dt 1e-4 for `steps` steps with the
+    learned opening test (trained on this run unless a model is given),
+    split precision, walk stack tuned, CUDA-graph steps.  Every `every`
+    steps: the rms / max force error against the direct sum (FP32 pairs,
+    FP64 sums) on 4,096 targets, the leaves at the 21-level key limit, and
+    |L|; energy (exact pair potential, FP32 pair terms, about a minute at
+    this N) at the start and the end when `energy`."""
+    arrs = ic.uniform_ball(n, seed=4)
+    eps, dt = 0.001, 1e-4
+    mtot = float(np.sum(arrs[6], dtype=np.float64))
+    rec = {"n": n, "eps": eps, "dt": dt, "steps": steps, "mac": "learned", "budget": budget, "timeline": []}
+    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=eps, theta=0.6, dt=dt), leaf_capacity=32, device=dev,
+                         timing=True) as sim:
+        sim.set_particles_f32(*arrs)
+        sim.prime()
+        t0 = time.perf_counter()
+        if model is None:
+            rec["train"] = sim.lmac_train(snapshots=4, steps_between=1, dt=dt, pairs=1 << 21, epochs=4, batch=8192,
+                                          seed=1)
+            model = sim.lmac_get_model()
+            sim.set_particles_f32(*arrs)
+            sim.prime()
+        rec["train_wall_s"] = time.perf_counter() - t0
+        sim.lmac_set_model(*model)
+        sim.set_opts(mac=pkg.MAC_LEARNED)
+        sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=1.5e-3)
+        sim.prime()
+        d0 = sim.diagnostics(exact_potential=2 if energy else 0)
+        ms = 0.0
+        for k in range(steps // every):
+            sim.reset_cumulative()
+            sim.step(every, dt)
+            st = sim.stats()
+            ms += st["cum_ms_step"]
+            fe = sim.force_error(4096, seed=100 + k, fp64_pairs=False)
+            d = sim.diagnostics(exact_potential=0)
+            rec["timeline"].append({"step": (k + 1) * every, "ms_per_step": st["cum_ms_step"] / every,
+                                    "force_err_rms": fe["rms"], "force_err_max": fe["max"],
+                                    "depth_limited_leaves": st["depth_limited_leaves"], "levels": st["levels"],
+                                    "L_mag": float(np.linalg.norm(d["L"])), "lmac_active": st["lmac_active"]})
+        st = sim.stats()
+        d1 = sim.diagnostics(exact_potential=2 if energy else 0)
+    rec["ms_per_step"] = ms / steps
+    rec["value"] = n / (rec["ms_per_step"] * 1e-3)
+    rec["lmac_reverted"] = bool(st["lmac_reverted"])
+    rec["lmac_checks"] = st["lmac_checks"]
+    rec["L_scale"] = float(np.sqrt(2.0 * mtot * max(d1["kinetic"], 1e-300)))  # |L| per unit length at the end
+    if energy:
+        rec.update(drift(d0, d1, mtot))
+    else:
+        rec["energy_drift"] = None
+        rec["energy_drift_note"] = "exact potential at 16.8M takes about a minute; run --workload collapse16m"
+    return rec
+
+
+def cpu_error(O, x, y, z, m, eps, acc, ntargets=4096, seed=7):
+    """rms / max relative error of the oracle's sampled Barnes-Hut
+    accelerations against its FP64 direct sum, on ntargets of the walked
+    targets (the accuracy the CPU arm runs at)."""
+    ax, ay, az = acc
+    walked = np.flatnonzero(np.isfinite(ax))
+    rng = np.random.default_rng(seed)
+    t = np.sort(rng.choice(walked, size=min(ntargets, walked.size), replace=False))
+    dx, dy, dz = O.direct_targets(x, y, z, m, 1.0, eps, t)
+    ref = np.sqrt(dx ** 2 + dy ** 2 + dz ** 2)
+    e = np.sqrt((ax[t] - dx) ** 2 + (ay[t] - dy) ** 2 + (az[t] - dz) ** 2) / ref
+    return {"rms": float(np.sqrt(np.mean(e ** 2))), "max": float(e.max()), "targets": int(t.size)}
+
+
 def cpu_baseline(orc, arrs, eps, theta, ncrit, target_s=15.0):
-    """Oracle on the host cores: full tree + a strided sample of leaf groups."""
+    """Oracle on the host cores: full tree + a strided sample of leaf groups,
+    and the rms error of that sample against the FP64 direct sum."""
     O = orc.Oracle()
     x, y, z, _, _, _, m = (a.astype(np.float64) for a in arrs)
     n = len(x)
@@ -195,38 +323,67 @@ def cpu_baseline(orc, arrs, eps, theta, ncrit, target_s=15.0):
         stride = max(1, stride // 4)
         build_ms, walk_ms, frac, _ = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride)
     step_ms = build_ms + walk_ms / max(frac, 1e-12)
+    _, _, _, _, acc = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, max(stride, 16), with_acc=True)
     return {"value": n / (step_ms * 1e-3), "unit": "particle-steps/s", "cores": O.num_threads(),
-            "kind": "port", "step_ms_extrapolated": step_ms,
+            "kind": "port", "step_ms_extrapolated": step_ms, "theta": theta, "leaf_capacity": ncrit,
+            "force_err": cpu_error(O, x, y, z, m, eps, acc),
             "sample": f"N={n}: full FP64 tree build ({build_ms:.0f} ms) + grouped walk over every "
                       f"{stride}-th leaf group ({100 * frac:.1f}% of particles, {walk_ms:.0f} ms), "
                       f"extrapolated to one full force evaluation"}
 
 
+# The theta test's setting at the 1e-3 rms target on the galaxy (the GPU
+# theta arm calibrates to it: theta 0.625 at leaf capacity 32); the CPU arm
+# runs the reference's algorithm at that setting and states its own error.
+REF_THETA, REF_LEAF = 0.625, 32
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle port of Tree.cpp / Solvers.cpp,
+    OpenMP on every host core) on this config.  Each timed step is a bounded
+    sample of one KDK force evaluation: the full FP64 tree build plus the
+    grouped walk over every k-th leaf group; the line's value extrapolates it
+    to the whole walk ("extrapolated": true), ms_per_step is the sample's own
+    wall time."""
     if rank != 0:
         return 0
     orc = ge.load_oracle()
     orc.build_oracle()
     ic = __import__(ge.PKG_NAME + ".ic", fromlist=["ic"]) if ge.load_package() else None
-    arrs, eps, dt, theta, ncrit = make_inputs(ic, args.workload)
+    arrs, eps, dt, _, _ = make_inputs(ic, args.workload)
+    theta, ncrit = REF_THETA, REF_LEAF
     O = orc.Oracle()
     x, y, z, _, _, _, m = (a.astype(np.float64) for a in arrs)
     n = len(x)
     stride = max(1, int(n // 16384))
-    times = []
+    sample_ms, full_ms, parts = [], [], []
     for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
         build_ms, walk_ms, frac, _ = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride)
+        wall = 1e3 * (time.perf_counter() - t0)
         if k >= args.warmup:
-            times.append(build_ms + walk_ms / max(frac, 1e-12))
-    step_ms = float(np.mean(times))
+            sample_ms.append(wall)
+            full_ms.append(build_ms + walk_ms / max(frac, 1e-12))
+            parts.append((build_ms, walk_ms, frac))
+    step_ms = float(np.mean(full_ms))
     value = n / (step_ms * 1e-3)
+    _, _, _, _, acc = O.time_sampled(x, y, z, m, 1.0, eps, theta, ncrit, stride, with_acc=True)
+    err = cpu_error(O, x, y, z, m, eps, acc)
+    b, w, f = (float(np.mean([p[i] for p in parts])) for i in range(3))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-            "scaling": "replicas", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "n": n, "theta": theta, "eps": eps, "leaf_capacity": ncrit},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(sample_ms)),
+            "higher_is_better": True, "scaling": "replicas", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "extrapolated": True,
+            "config": {"workload": args.workload, "n": n, "theta": theta, "eps": eps, "leaf_capacity": ncrit,
+                       "force_err_rms": err["rms"], "force_err_max": err["max"], "force_err_targets": err["targets"],
+                       "sampled_fraction": f, "ms_build": b, "ms_walk_sampled": w,
+                       "ms_per_step_extrapolated": step_ms,
+                       "implementation": "oracle/ngrav_oracle.c, the C restatement of Tree.cpp + Solvers.cpp "
+                                         "(the reference's own sources are not on this machine)"},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": O.num_threads(), "kind": "port",
                              "sample": f"each step: full FP64 tree build + grouped walk over every {stride}-th "
-                                       f"leaf group, extrapolated to one full KDK force evaluation"},
+                                       f"leaf group ({100 * f:.2f}% of particles), extrapolated to one full KDK "
+                                       f"force evaluation"},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -273,11 +430,14 @@ def job_value(n, world, ms_max):
     return world * n / (ms_max * 1e-3)
 
 
-def timed(sim, steps, warmup, dt, clocks=None, dist=None):
+def timed(sim, steps, warmup, dt, clocks=None, dist=None, diag=None):
     """W untimed steps, then exactly K steps between barriers (each
     ngrav_gpu_step call returns with its stream synchronised); the time is the
-    device time of the K steps on the engine's stream."""
+    device time of the K steps on the engine's stream.  diag: a callable run
+    just before and just after the K steps (outside the timed region); its
+    two results are returned too."""
     sim.step(warmup, dt)
+    d0 = diag() if diag else None
     if dist is not None:
         dist.barrier()
     if clocks:
@@ -288,7 +448,24 @@ def timed(sim, steps, warmup, dt, clocks=None, dist=None):
     clk = clocks.stop() if clocks else None
     if dist is not None:
         dist.barrier()
+    d1 = diag() if diag else None
+    if diag:
+        return st, st["cum_ms_step"] / steps, clk, (d0, d1)
     return st, st["cum_ms_step"] / steps, clk
+
+
+def drift(d0, d1, mtot):
+    """Relative conservation errors between two FP64 diagnostics: energy
+    (E1 - E0) / |E0|; momentum |P1 - P0| over the momentum scale
+    sqrt(2 M K0) (the system's net momentum is ~0 in the COM frame);
+    angular momentum |L1 - L0| / |L0|."""
+    dP = float(np.linalg.norm(np.subtract(d1["P"], d0["P"])))
+    L0 = float(np.linalg.norm(d0["L"]))
+    return {"energy_drift": (d1["energy"] - d0["energy"]) / abs(d0["energy"]),
+            "momentum_drift": dP / np.sqrt(2.0 * mtot * d0["kinetic"]),
+            "angular_momentum_drift": float(np.linalg.norm(np.subtract(d1["L"], d0["L"]))) / L0 if L0 > 0 else None,
+            "potential": "exact pair sum, FP32 pair terms, FP64 sums" if d0["potential_exact"] == 2 else
+                         ("exact pair sum, FP64" if d0["potential_exact"] == 1 else "none")}
 
 
 def hbm_peak():
@@ -359,8 +536,10 @@ def main():
     ap.add_argument("--precision", default="split", choices=["split", "plain"])
     ap.add_argument("--leaf-grid", default="16,24,32,40,48",
                     help="leaf capacities tried per arm (comma list; one value fixes it)")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the compact records of the other BASELINE configs (C2, C3, C5)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -371,6 +550,19 @@ def main():
     dev = local
     if WORKLOADS[args.workload][0] == "ensemble":
         return run_ensemble(args, pkg, ic, rank, world, dev)
+    if args.workload == "plummer1m":
+        if rank == 0:
+            print(json.dumps({"metric": "C2 Plummer 1M: plain FP32 vs split precision + Kahan, 100 KDK steps",
+                              "config": {"workload": "plummer1m", **precision_run(pkg, ic, dev, steps=100)}}),
+                  flush=True)
+        return 0
+    if args.workload == "collapse16m":
+        r = collapse_run(pkg, ic, dev, energy=True)
+        if rank == 0:
+            print(json.dumps({"metric": "C5 cold collapse 16.8M, learned test, 200 KDK steps", "value": r["value"],
+                              "unit": "particle-steps/s", "ms_per_step": r["ms_per_step"],
+                              "config": {"workload": "collapse16m", **r}}), flush=True)
+        return 0
     arrs, eps, dt, theta0, ncrit = make_inputs(ic, args.workload)
     n = len(arrs[0])
     prec = pkg.PRECISION_SPLIT if args.precision == "split" else pkg.PRECISION_PLAIN
@@ -462,7 +654,9 @@ def main():
     restart(ncrit_t)
     sim.set_opts(theta=theta, mac=pkg.MAC_GEOMETRIC)
     ws_t = pick_walk_stack()
-    st_g, ms_g, clk_g = timed(sim, args.steps, args.warmup, dt, None if learned else clocks, dist)
+    mtot = float(np.sum(arrs[6], dtype=np.float64))
+    diag2 = lambda: sim.diagnostics(exact_potential=2)  # noqa: E731
+    st_g, ms_g, clk_g, dg = timed(sim, args.steps, args.warmup, dt, None if learned else clocks, dist, diag=diag2)
     ms_g = replica_max(ms_g, dist, f"cuda:{dev}")
     fe_g = error_at(sim)
     arm_theta = {"theta": theta, "leaf_capacity": ncrit_t, "walk_stack": ws_t, "value": job_value(n, world, ms_g),
@@ -472,7 +666,7 @@ def main():
                  "p2c_terms_per_step": st_g["cum_p2c_terms"] / max(1, st_g["cum_evals"]),
                  "ms_walk_per_step": st_g["cum_ms_walk"] / max(1, st_g["cum_evals"]),
                  "ms_force_per_step": st_g["cum_ms_force"] / max(1, st_g["cum_evals"]),
-                 "ms_phases_last_eval": phases(st_g), "calibration": cal_theta}
+                 "ms_phases_last_eval": phases(st_g), "calibration": cal_theta, **drift(dg[0], dg[1], mtot)}
 
     # ---- learned arm (the method) ----
     ws_l = ws_t
@@ -483,10 +677,10 @@ def main():
         sim.lmac_set_opts(budget=budget, check_every=10, check_targets=4096, revert_rms=TARGET_RMS * 1.5)
         ws_l = pick_walk_stack()
         sim.lmac_reset()
-        st, ms_step, clk = timed(sim, args.steps, args.warmup, dt, clocks, dist)
+        st, ms_step, clk, dl = timed(sim, args.steps, args.warmup, dt, clocks, dist, diag=diag2)
         fe = error_at(sim)
     else:
-        st, ms_step, clk, fe = st_g, ms_g, clk_g, fe_g
+        st, ms_step, clk, fe, dl = st_g, ms_g, clk_g, fe_g, dg
     ms_max = replica_max(ms_step, dist, f"cuda:{dev}")
     value = job_value(n, world, ms_max)
 
@@ -511,23 +705,29 @@ def main():
     fin = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) for a in hin]
     dout = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in hout]
     L = sim.L
-    t_e2e = []
+    t_e2e, t_parts = [], []
     for k in range(1 + args.e2e_steps):
         t0 = time.perf_counter()
         rc = L.ngrav_gpu_set_state_f32(sim.h, *fin)
-        rc |= L.ngrav_gpu_step(sim.h, 1, ctypes.c_double(dt))
-        rc |= L.ngrav_gpu_get_state(sim.h, *dout)
         t1 = time.perf_counter()
+        rc |= L.ngrav_gpu_step(sim.h, 1, ctypes.c_double(dt))
+        t2 = time.perf_counter()
+        rc |= L.ngrav_gpu_get_state(sim.h, *dout)
+        t3 = time.perf_counter()
         if rc:
             raise RuntimeError("e2e call failed: " + L.ngrav_gpu_last_error(sim.h).decode())
         if k > 0:
-            t_e2e.append(t1 - t0)
+            t_e2e.append(t3 - t0)
+            t_parts.append((t1 - t0, t2 - t1, t3 - t2))
         for a, b in zip(hin, hout):
             a[:] = b  # the next step starts from this step's result
     e2e_ms = 1e3 * float(np.mean(t_e2e))
     e2e_ms = replica_max(e2e_ms, dist, f"cuda:{dev}")
+    parts = [1e3 * float(np.mean([p[i] for p in t_parts])) for i in range(3)]
     e2e = {"value": job_value(n, world, e2e_ms), "unit": "particle-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
-           "d2h_bytes_per_step": 6 * 8 * n, "ms_per_step": e2e_ms,
+           "d2h_bytes_per_step": 6 * 8 * n, "ms_per_step": e2e_ms, "steps": args.e2e_steps,
+           "ms_set_state": parts[0], "ms_step": parts[1], "ms_get_state": parts[2],
+           "h2d_gbs": 6 * 4 * n / (parts[0] * 1e-3) / 1e9, "d2h_gbs": 6 * 8 * n / (parts[2] * 1e-3) / 1e9,
            "call": "ngrav_gpu_set_state_f32 + ngrav_gpu_step(1) + ngrav_gpu_get_state (pinned host buffers)"}
 
     cpu = None
@@ -555,7 +755,8 @@ def main():
                "list_entries_per_step": st["far_entries"] + st["near_entries"],
                "mac_tests_per_step": st["mac_tests"], "walk_stack_max": st["walk_stack_max"],
                "leaves": st["leaves"], "nodes": st["nodes"], "ms_phases_last_eval": phases(st),
-               "graph_replays": st["graph_replays"], "theta_arm": arm_theta}
+               "graph_replays": st["graph_replays"], "theta_arm": arm_theta, **drift(dl[0], dl[1], mtot),
+               "drift_over": f"the {args.steps} timed steps"}
         if learned:
             cfg["learned"] = {"budget": budget, "calibration": cal_budget, "train": train,
                               "queries_last_eval": st["lmac_queries"], "accepts_last_eval": st["lmac_accepts"],
@@ -581,8 +782,23 @@ def main():
             "roofline_p2p": p2p_phase_roofline(pkg, ic, dev, peak, prec),
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": st["cum_launches"], "clocks": clk,
         }
-        print(json.dumps(line), flush=True)
     sim.close()
+    if rank == 0 and world == 1 and not args.no_configs:
+        # compact records of the other configs of the task (untimed by the
+        # headline): C2 plain vs split precision, C3 ensemble, C5 cold collapse
+        extra = {}
+        for name, fn in (("C2_plummer1m_precision", lambda: precision_run(pkg, ic, dev, steps=100)),
+                         ("C3_ensemble512", lambda: ensemble_run(pkg, ic, dev, steps=10, warmup=3, tune_reps=1)),
+                         ("C5_collapse16m", lambda: collapse_run(pkg, ic, dev, budget=budget or 3.5e-4))):
+            t0 = time.perf_counter()
+            try:
+                extra[name] = fn()
+            except Exception as exc:  # a side record must not sink the headline line
+                extra[name] = {"error": str(exc)}
+            extra[name]["wall_s"] = time.perf_counter() - t0
+        line["configs"] = extra
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
