@@ -10,29 +10,31 @@
 // zero for eps > 0 and masked for eps == 0).
 //
 // GB300 mapping.  One warp per group (dynamic scheduling), lane = (target t,
-// slice s): nt targets x floor(32/nt) source slices, each slice a contiguous
-// run of the staged sources (odd length, so the slices of a quarter-warp
-// read distinct bank groups), walked four at a time; slices are summed at
+// slice s): nt targets x floor(32/nt) source slices; slices are summed at
 // the end of the group.  A group's targets run in blocks of up to 64, each
 // in one or two passes over every staged chunk (split to keep the lanes
 // busy: 20 targets as 4 x 8 + 16 x 2 slices), the second pass's sums parked
-// in shared memory; 80 registers and about 9 KiB of shared memory per warp
-// keep 6 CTAs of 4 warps per SM.
+// in shared memory.  The pair arithmetic runs on Blackwell's packed FP32
+// pipe (add / mul / fma .f32x2): each lane takes two sources per step, so
+// twelve pair operations issue as six instructions and the kernel is bound
+// by the FMA pipe rather than by issue slots, leaving the staging work its
+// own issue slots.  Staged sources are therefore kept as pairs, {x0 x1 y0
+// y1}{z0 z1 m0 m1}, and far records as pairs of records likewise.
 // Far records are staged 32 at a time into shared memory in the group's
 // frame; the records of the next batch and the node ids of the one after
 // are loaded while a batch is evaluated, so no batch waits on a list-id ->
 // record load chain.  Near leaves are staged by TMA bulk copies
 // (cp.async.bulk completing on an mbarrier with a bounded wait), one copy
 // per run of leaves whose particles are contiguous (leaves are in key order,
-// so siblings met together form one run), into a 5 KiB shared-memory
+// so siblings met together form one run), into a 6 KiB shared-memory
 // buffer, each batch as many leaves (up to 32) as fit by their actual
-// counts; the first near batch is in flight during the far field, and each
-// next batch's leaf records load while a batch is evaluated.  (A second
-// buffer would overlap copy and compute within the warp, but halves the
-// resident warps; measured slower.)  In SPLIT precision the staged sources
-// then move from their leaves' frames into the group's (each slot knows its
-// leaf from a byte map written at staging), and each lane's partial sums
-// are Kahan compensated once per staged chunk.
+// counts; the first near batch is in flight during the far field, and the
+// next batch's leaf records are copied into shared memory (cp.async) while
+// a batch is evaluated.  A pass over each landed batch then pairs the
+// sources up in place and, in SPLIT precision, moves them from their
+// leaves' frames into the group's (each slot finds its leaf from a bit mask
+// of the leaves' first slots), and each lane's partial sums are Kahan
+// compensated once per staged chunk.
 #include "engine.cuh"
 #include "softening.cuh"
 
@@ -40,25 +42,35 @@ namespace ngrav {
 
 constexpr int kEvalWarps = 4;
 constexpr int kEvalThreads = kEvalWarps * 32;
-constexpr int kSrcCap = 320;                  // sources per staging buffer (5 KiB)
-constexpr int kBuffers = 1;                   // staging buffers per warp (2 halves occupancy)
+constexpr int kEvalMinBlocks = 5;             // CTAs per SM (96 registers per thread)
+constexpr int kSrcCap = 384;                  // sources per staging buffer (6 KiB; even: a pad slot for odd counts)
 constexpr unsigned kWaitLimit = 1u << 26;     // bounded mbarrier polling
+constexpr float kFarPad = 1e18f;              // position of the zero record that pads an odd far batch
 
 struct __align__(128) EvalSmem {
-    float4 src[kBuffers][kSrcCap];            // TMA destinations
-    float4 farA[32];                          // far batch: COM in the group frame, mass
-    float4 farB[32];                          //   Qxx Qyy Qxy Qxz
-    float2 farQ[32];                          //   Qyz, Qzz = -(Qxx + Qyy)
+    float4 src[kSrcCap];                      // TMA destination; then source pairs {x0 x1 y0 y1}{z0 z1 m0 m1}
+    float4 farX[16];                          // far record pairs in the group frame: x0 x1 y0 y1
+    float4 farZ[16];                          //   z0 z1 m0 m1
+    float4 farQ0[16];                         //   Qxx0 Qxx1 Qyy0 Qyy1
+    float4 farQ1[16];                         //   Qxy0 Qxy1 Qxz0 Qxz1
+    float4 farQ2[16];                         //   Qyz0 Qyz1 Qzz0 Qzz1 (Qzz = -(Qxx + Qyy))
     float red[3][32];                         // slice reduction
     float4 pass_tgt[32];                      // second pass of a target block: target, packed lane map
     float4 pass_acc[32];                      //   running sums ax ay az, compensation cx
     float2 pass_cmp[32];                      //   compensation cy cz
-    float4 shift[kBuffers][32];               // near-leaf frame shift (SPLIT)
-    int start[kBuffers][32];
-    int pre[kBuffers][33];
-    unsigned long long bar[2];
-    unsigned char owner[kSrcCap];             // staged slot -> its leaf's lane in the batch (SPLIT)
+    float4 shift[32];                         // staged leaves' frame shifts (SPLIT), by rank
+    float4 nwc[32];                           // next near batch's leaf records (cp.async): wC
+    float4 nhi[32];                           //   centre hi (SPLIT)
+    float4 nlo[32];                           //   centre lo (SPLIT)
+    float4 gch, gcl;                          // the group leaf's centre, hi and lo (SPLIT)
+    int first[32];                            // staged leaves' first slots, by rank
+    int nleaf;                                // non-empty leaves in the staged batch
+    unsigned long long bar;
+    unsigned long long npairs, nterms;        // interaction counters of this warp
 };
+// kEvalMinBlocks CTAs of kEvalWarps warps fit one SM's 228 KiB of shared
+// memory (1 KiB of it reserved per CTA).
+static_assert(kEvalMinBlocks * (kEvalWarps * sizeof(EvalSmem) + 1024) <= 228 * 1024, "eval smem per SM");
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -110,9 +122,9 @@ __device__ __forceinline__ int excl_scan(int v, int lane, int& total) {
 
 // Lane mapping for a block of nt <= 32 targets: lane = (target t, slice s),
 // t = lane % nt, s = lane / nt, S = floor(32 / nt) slices.  All lanes of a
-// slice read the same source (shared-memory broadcast).  P2P slices are
-// contiguous runs of the staged sources (p2p_chunk); P2C slices take records
-// s, s + S, s + 2S, ... of a 32-record batch.
+// slice read the same source pair (shared-memory broadcast).  P2P slices are
+// contiguous runs of the staged source pairs (p2p_chunk); P2C slices take
+// record pairs s, s + S, s + 2S, ... of a 32-record batch.
 struct Lane {
     float tx, ty, tz;
     int sl, S, nt;
@@ -231,152 +243,230 @@ __device__ __forceinline__ void for_passes(Lane& g, bool two, EvalSmem& sm, int 
     }
 }
 
+// Packed FP32 pair arithmetic (two lanes of one register pair per op).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// Two sources {x0 x1 y0 y1}{z0 z1 m0 m1} against one target (given negated
+// and duplicated): the reference's softened pair
+// (Solvers.cpp:19-38, AccumPairPlummer) for each, FP32.
 // SOFT: 0 Plummer, 1 Plummer with eps = 0 (the self pair gives 0), 2 spline.
 template <int SOFT>
-__device__ __forceinline__ void p2p_pair(const float4& a, float tx, float ty, float tz, float eps2, float ih,
-                                         float& px, float& py, float& pz) {
-    const float dx = a.x - tx, dy = a.y - ty, dz = a.z - tz;
-    float f;
+__device__ __forceinline__ void p2p_pair2(const float4& P, const float4& Q, float2 ntx, float2 nty, float2 ntz,
+                                          float2 e2, float ih, float2& ax, float2& ay, float2& az) {
+    const float2 dx = add2(make_float2(P.x, P.y), ntx);
+    const float2 dy = add2(make_float2(P.z, P.w), nty);
+    const float2 dz = add2(make_float2(Q.x, Q.y), ntz);
+    const float2 m = make_float2(Q.z, Q.w);
+    float2 f;
     if (SOFT == 2) {
-        f = pair_factor<kSoftSpline>(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), a.w, 0.f, ih);
+        const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+        f = make_float2(pair_factor<kSoftSpline>(r2.x, m.x, 0.f, ih), pair_factor<kSoftSpline>(r2.y, m.y, 0.f, ih));
     } else {
-        const float r = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-        const float ir = rsqrtf(r);
-        f = a.w * (ir * ir * ir);
-        if (SOFT == 1) f = r > 0.f ? f : 0.f;
-    }
-    px = fmaf(f, dx, px);
-    py = fmaf(f, dy, py);
-    pz = fmaf(f, dz, pz);
-}
-
-// One staged chunk of ns sources against the lane's target.  Slice s takes a
-// contiguous run of len = ceil(ns / S) sources (rounded up to odd: the S
-// slices of a quarter-warp then read distinct shared-memory bank groups in
-// the same LDS.128), walked four at a time with immediate offsets from one
-// pointer, in two independent accumulation chains.
-template <bool SPLIT, int SOFT>
-__device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s_src, int ns, float eps2, float ih) {
-    if (!g.active) return;
-    float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-    const float tx = g.tx, ty = g.ty, tz = g.tz;
-    const int len = ((ns + g.S - 1) / g.S) | 1;
-    const int b = min(ns, g.sl * len);
-    const float4* p = s_src + b;
-    const float4* const pe = s_src + min(ns, b + len);
-    for (; p + 4 <= pe; p += 4) {
-        const float4 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3];
-        p2p_pair<SOFT>(a0, tx, ty, tz, eps2, ih, px, py, pz);
-        p2p_pair<SOFT>(a1, tx, ty, tz, eps2, ih, qx, qy, qz);
-        p2p_pair<SOFT>(a2, tx, ty, tz, eps2, ih, px, py, pz);
-        p2p_pair<SOFT>(a3, tx, ty, tz, eps2, ih, qx, qy, qz);
-    }
-    for (; p < pe; ++p) p2p_pair<SOFT>(p[0], tx, ty, tz, eps2, ih, px, py, pz);
-    accumulate<SPLIT>(g, px + qx, py + qy, pz + qz);
-}
-
-template <bool SPLIT, bool QUAD, int SOFT>
-__device__ __forceinline__ void p2c_chunk(Lane& g, const float4* __restrict__ fA, const float4* __restrict__ fB,
-                                          const float2* __restrict__ fQ, int nf, float eps2, float ih) {
-    if (!g.active) return;
-    float px = 0.f, py = 0.f, pz = 0.f;
-    const float tx = g.tx, ty = g.ty, tz = g.tz;
-    for (int f = g.sl; f < nf; f += g.S) {
-        const float4 A = fA[f];
-        const float dx = A.x - tx, dy = A.y - ty, dz = A.z - tz;
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float fm = pair_factor<SOFT == 2 ? kSoftSpline : kSoftPlummer>(r2, A.w, eps2, ih);
-        if (QUAD) {
-            const float4 B = fB[f];
-            const float2 Q = fQ[f];  // Qyz, Qzz
-            const float qdx = fmaf(B.x, dx, fmaf(B.z, dy, B.w * dz));
-            const float qdy = fmaf(B.z, dx, fmaf(B.y, dy, Q.x * dz));
-            const float qdz = fmaf(B.w, dx, fmaf(Q.x, dy, Q.y * dz));
-            const float qd2 = fmaf(dx, qdx, fmaf(dy, qdy, dz * qdz));
-            const float ir = rsqrtf(r2);
-            const float ir2 = ir * ir;
-            const float ir5 = ir2 * ir2 * ir;
-            // monopole and the radial quadrupole term share one multiplier of d
-            const float c = fm + 2.5f * qd2 * (ir5 * ir2);
-            px = fmaf(-ir5, qdx, fmaf(c, dx, px));
-            py = fmaf(-ir5, qdy, fmaf(c, dy, py));
-            pz = fmaf(-ir5, qdz, fmaf(c, dz, pz));
-        } else {
-            px = fmaf(fm, dx, px);
-            py = fmaf(fm, dy, py);
-            pz = fmaf(fm, dz, pz);
+        const float2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+        const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        f = mul2(m, mul2(mul2(ir, ir), ir));
+        if (SOFT == 1) {
+            f.x = r2.x > 0.f ? f.x : 0.f;
+            f.y = r2.y > 0.f ? f.y : 0.f;
         }
     }
-    accumulate<SPLIT>(g, px, py, pz);
+    ax = fma2(f, dx, ax);
+    ay = fma2(f, dy, ay);
+    az = fma2(f, dz, az);
 }
 
-// One near leaf's info (lane = list entry), loaded into registers.  The
-// leaf centre's double-float halves are kept as loaded: the frame shift is
-// formed only when the batch is staged, a batch later, so these loads never
-// stall the batch being computed.
-struct NearInfo {
-    int start, cnt;
-    float4 h, l;
-};
-
-// Publish a batch's info to buffer `b` and start its TMA copies: one bulk
-// copy per run of leaves whose particles are contiguous in memory (leaves
-// are in key order, so siblings met together form one run), issued by the
-// run's first lane.  In SPLIT precision each lane also forms its leaf's
-// frame shift and marks the staged slots of its leaf in `owner`.  Returns
-// the number of staged sources.
-template <bool SPLIT>
-__device__ __forceinline__ int stage_batch(EvalSmem& sm, int b, const NearInfo& in, int lane,
-                                          const float4* __restrict__ src, const float4& gchi, const float4& gclo) {
-    int tot;
-    const int ex = excl_scan(in.cnt, lane, tot);
-    sm.start[b][lane] = in.start;
-    sm.pre[b][lane] = ex;
-    if (lane == 31) sm.pre[b][32] = tot;
-    if (SPLIT) {
-        sm.shift[b][lane] = make_float4((in.h.x - gchi.x) + (in.l.x - gclo.x), (in.h.y - gchi.y) + (in.l.y - gclo.y),
-                                        (in.h.z - gchi.z) + (in.l.z - gclo.z), 0.f);
-        for (int k = 0; k < in.cnt; ++k) sm.owner[ex + k] = (unsigned char)lane;
+// One staged chunk of np source pairs against the lane's target.  Slice s
+// takes a contiguous run of len = ceil(np / S) pairs (rounded up to odd: the
+// slices of a quarter-warp then read distinct shared-memory bank groups in
+// the same LDS.128), walked four pairs at a time with immediate offsets from
+// one pointer, in two independent accumulation chains.
+template <bool SPLIT, int SOFT>
+__device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s2, int np, float eps2, float ih) {
+    if (!g.active) return;
+    const float2 ntx = dup2(-g.tx), nty = dup2(-g.ty), ntz = dup2(-g.tz), e2 = dup2(eps2);
+    float2 ax = dup2(0.f), ay = ax, az = ax, bx = ax, by = ax, bz = ax;
+    const int len = ((np + g.S - 1) / g.S) | 1;
+    const int b = min(np, g.sl * len);
+    const float4* p = s2 + 2 * b;
+    const float4* const pe = s2 + 2 * min(np, b + len);
+    for (; p + 8 <= pe; p += 8) {
+        const float4 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3], a4 = p[4], a5 = p[5], a6 = p[6], a7 = p[7];
+        p2p_pair2<SOFT>(a0, a1, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a2, a3, ntx, nty, ntz, e2, ih, bx, by, bz);
+        p2p_pair2<SOFT>(a4, a5, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a6, a7, ntx, nty, ntz, e2, ih, bx, by, bz);
     }
+    for (; p < pe; p += 2) p2p_pair2<SOFT>(p[0], p[1], ntx, nty, ntz, e2, ih, ax, ay, az);
+    const float2 sx = add2(ax, bx), sy = add2(ay, by), sz = add2(az, bz);
+    accumulate<SPLIT>(g, sx.x + sx.y, sy.x + sy.y, sz.x + sz.y);
+}
+
+// One far batch of np record pairs against the lane's target: the softened
+// monopole of each node's mass at its COM plus the unsoftened quadrupole
+// (Solvers.cpp:147-179, AddQuadrupole), the two sharing one multiplier of
+// the offset.  Packed FP32 over the two records of a pair.
+template <bool SPLIT, bool QUAD, int SOFT>
+__device__ __forceinline__ void p2c_chunk(Lane& g, const EvalSmem& sm, int np, float eps2, float ih) {
+    if (!g.active) return;
+    const float2 ntx = dup2(-g.tx), nty = dup2(-g.ty), ntz = dup2(-g.tz), e2 = dup2(eps2);
+    float2 ax = dup2(0.f), ay = ax, az = ax;
+    for (int k = g.sl; k < np; k += g.S) {
+        const float4 X = sm.farX[k], Z = sm.farZ[k];
+        const float2 dx = add2(make_float2(X.x, X.y), ntx);
+        const float2 dy = add2(make_float2(X.z, X.w), nty);
+        const float2 dz = add2(make_float2(Z.x, Z.y), ntz);
+        const float2 m = make_float2(Z.z, Z.w);
+        const float2 r2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+        float2 fm;
+        if (SOFT == 2) {
+            fm = make_float2(pair_factor<kSoftSpline>(r2.x, m.x, eps2, ih), pair_factor<kSoftSpline>(r2.y, m.y, eps2, ih));
+        } else {
+            const float2 re = add2(r2, e2);
+            const float2 is = make_float2(rsqrtf(re.x), rsqrtf(re.y));
+            fm = mul2(m, mul2(mul2(is, is), is));
+        }
+        if (QUAD) {
+            const float4 Q0 = sm.farQ0[k], Q1 = sm.farQ1[k], Q2 = sm.farQ2[k];
+            const float2 qxx = make_float2(Q0.x, Q0.y), qyy = make_float2(Q0.z, Q0.w);
+            const float2 qxy = make_float2(Q1.x, Q1.y), qxz = make_float2(Q1.z, Q1.w);
+            const float2 qyz = make_float2(Q2.x, Q2.y), qzz = make_float2(Q2.z, Q2.w);
+            const float2 qdx = fma2(qxx, dx, fma2(qxy, dy, mul2(qxz, dz)));
+            const float2 qdy = fma2(qxy, dx, fma2(qyy, dy, mul2(qyz, dz)));
+            const float2 qdz = fma2(qxz, dx, fma2(qyz, dy, mul2(qzz, dz)));
+            const float2 qd2 = fma2(dx, qdx, fma2(dy, qdy, mul2(dz, qdz)));
+            const float2 ir = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 ir2 = mul2(ir, ir);
+            const float2 ir5 = mul2(mul2(ir2, ir2), ir);
+            const float2 nir5 = make_float2(-ir5.x, -ir5.y);
+            // monopole and the radial quadrupole term share one multiplier of d
+            const float2 c = fma2(mul2(dup2(2.5f), qd2), mul2(ir5, ir2), fm);
+            ax = fma2(nir5, qdx, fma2(c, dx, ax));
+            ay = fma2(nir5, qdy, fma2(c, dy, ay));
+            az = fma2(nir5, qdz, fma2(c, dz, az));
+        } else {
+            ax = fma2(fm, dx, ax);
+            ay = fma2(fm, dy, ay);
+            az = fma2(fm, dz, az);
+        }
+    }
+    accumulate<SPLIT>(g, ax.x + ax.y, ay.x + ay.y, az.x + az.y);
+}
+
+// Far record of lane `lane` (the batch's entry b + lane; a zero record far
+// away when past the list) into its half of record pair lane / 2, in the
+// group frame.
+template <bool SPLIT, bool QUAD>
+__device__ __forceinline__ void stage_far(EvalSmem& sm, int lane, bool valid, const float4& A, const float4& B,
+                                          const float4& D) {
+    float x = kFarPad, y = kFarPad, z = kFarPad, m = 0.f;
+    float qxx = 0.f, qyy = 0.f, qxy = 0.f, qxz = 0.f, qyz = 0.f;
+    if (valid) {
+        x = A.x;
+        y = A.y;
+        z = A.z;
+        if (SPLIT) {
+            const float4 gh = sm.gch, gl = sm.gcl;
+            x = (A.x - gh.x) + (D.x - gl.x);
+            y = (A.y - gh.y) + (D.y - gl.y);
+            z = (A.z - gh.z) + (D.z - gl.z);
+        }
+        m = A.w;
+        if (QUAD) {
+            qxx = B.x;
+            qyy = B.y;
+            qxy = B.z;
+            qxz = B.w;
+            qyz = D.w;
+        }
+    }
+    const int k = lane >> 1, h = lane & 1;
+    float* fx = reinterpret_cast<float*>(&sm.farX[k]);
+    float* fz = reinterpret_cast<float*>(&sm.farZ[k]);
+    fx[h] = x;
+    fx[2 + h] = y;
+    fz[h] = z;
+    fz[2 + h] = m;
+    if (QUAD) {
+        float* q0 = reinterpret_cast<float*>(&sm.farQ0[k]);
+        float* q1 = reinterpret_cast<float*>(&sm.farQ1[k]);
+        float* q2 = reinterpret_cast<float*>(&sm.farQ2[k]);
+        q0[h] = qxx;
+        q0[2 + h] = qyy;
+        q1[h] = qxy;
+        q1[2 + h] = qxz;
+        q2[h] = qyz;
+        q2[2 + h] = -(qxx + qyy);
+    }
+}
+
+// Leaf records of the next near batch (lane = list entry; node < 0: past
+// the list) copied into shared memory by cp.async, so they cost no
+// registers while the batch before is evaluated and land long before they
+// are read.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void prefetch_near(EvalSmem& sm, const NodeArrays& T, int node, int lane) {
+    if (node >= 0) {
+        cp_async16(&sm.nwc[lane], &T.wC[node]);
+        if (SPLIT) {
+            cp_async16(&sm.nhi[lane], &T.chi[node]);
+            cp_async16(&sm.nlo[lane], &T.clo[node]);
+        }
+    } else {
+        sm.nwc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);  // count 0
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void prefetch_wait() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+}
+
+// Publish a batch (lane = leaf; cnt = 0 for lanes not staged; ex = the
+// leaf's first slot, tot = the staged total) and start its TMA copies: one
+// bulk copy per run of leaves whose particles are contiguous in memory
+// (leaves are in key order, so siblings met together form one run), issued
+// by the run's first lane.  The non-empty leaves' first slots and, in SPLIT
+// precision, frame shifts are stored by rank for the pairing pass.
+template <bool SPLIT>
+__device__ __forceinline__ void stage_batch(EvalSmem& sm, int start, int cnt, int ex, int tot, int lane,
+                                           const float4* __restrict__ src) {
+    const unsigned nz = __ballot_sync(0xffffffffu, cnt > 0);
+    if (cnt > 0) {
+        const int r = __popc(nz & ((1u << lane) - 1u));
+        sm.first[r] = ex;
+        if (SPLIT) {
+            const float4 h = sm.nhi[lane], l = sm.nlo[lane], gh = sm.gch, gl = sm.gcl;
+            sm.shift[r] = make_float4((h.x - gh.x) + (l.x - gl.x), (h.y - gh.y) + (l.y - gl.y),
+                                      (h.z - gh.z) + (l.z - gl.z), 0.f);
+        }
+    }
+    if (lane == 0) sm.nleaf = __popc(nz);
     if (tot > 0) {
         // run heads: a staged leaf that does not continue the previous lane's range
-        const int pend = __shfl_up_sync(0xffffffffu, in.start + in.cnt, 1);
-        const int pcnt = __shfl_up_sync(0xffffffffu, in.cnt, 1);
-        const bool head = in.cnt > 0 && (lane == 0 || pcnt == 0 || pend != in.start);
+        const int pend = __shfl_up_sync(0xffffffffu, start + cnt, 1);
+        const int pcnt = __shfl_up_sync(0xffffffffu, cnt, 1);
+        const bool head = cnt > 0 && (lane == 0 || pcnt == 0 || pend != start);
         const unsigned heads = __ballot_sync(0xffffffffu, head);
         const unsigned later = heads & ~(0xFFFFFFFFu >> (31 - lane));  // heads after this lane
         const int nxt = later ? __ffs(later) - 1 : 31;
         const int ex_next = __shfl_sync(0xffffffffu, ex, nxt);
         const int run_end = later ? ex_next : tot;
-        if (lane == 0) mbar_expect_tx(&sm.bar[b], (unsigned)tot * 16u);
+        if (lane == 0) mbar_expect_tx(&sm.bar, (unsigned)tot * 16u);
         __syncwarp();
         if (head) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            tma_load_1d(&sm.src[b][ex], src + in.start, (unsigned)(run_end - ex) * 16u, &sm.bar[b]);
+            tma_load_1d(&sm.src[ex], src + start, (unsigned)(run_end - ex) * 16u, &sm.bar);
         }
     }
     __syncwarp();
-    return tot;
-}
-
-// A leaf's staging info from its node id (-1: past the list, count 0).
-template <bool SPLIT>
-__device__ __forceinline__ NearInfo near_info_of(const NodeArrays& T, int node) {
-    NearInfo r;
-    r.start = 0;
-    r.cnt = 0;
-    r.h = make_float4(0.f, 0.f, 0.f, 0.f);
-    r.l = r.h;
-    if (node >= 0) {
-        const float4 Cw = T.wC[node];
-        r.start = __float_as_int(Cw.z);
-        r.cnt = __float_as_int(Cw.w) & 0xFFFFFF;
-        if (SPLIT) {
-            r.h = T.chi[node];
-            r.l = T.clo[node];
-        }
-    }
-    return r;
 }
 
 // The near list's node ids of entries pos .. pos+63 held in registers (w0:
@@ -423,34 +513,73 @@ __device__ __forceinline__ void near_advance(const ListBuffers& LB, NearWindow& 
     W.pos = np;
 }
 
-// Stage the longest prefix of the 32 leaves in `in` whose sources fit `cap`
-// (at least one: every leaf fits the buffer outside the big-leaf path).
-// Returns the staged source count; nb = leaves staged.
+// Stage the longest prefix of the 32 prefetched leaves whose sources fit
+// `cap` (at least one: every leaf fits the buffer outside the big-leaf
+// path).  Returns the staged source count; nb = leaves staged.
 template <bool SPLIT>
-__device__ __forceinline__ int stage_fitting(EvalSmem& sm, const NearInfo& in, int lane,
-                                             const float4* __restrict__ src, int cap, int& nb,
-                                             const float4& gchi, const float4& gclo) {
+__device__ __forceinline__ int stage_fitting(EvalSmem& sm, int lane, const float4* __restrict__ src, int cap,
+                                             int& nb) {
+    prefetch_wait();
+    const float4 Cw = sm.nwc[lane];
+    const int start = __float_as_int(Cw.z), c = __float_as_int(Cw.w) & 0xFFFFFF;
     int tot;
-    const int ex = excl_scan(in.cnt, lane, tot);
-    const bool fits = ex + in.cnt <= cap || lane == 0;
+    const int ex = excl_scan(c, lane, tot);
+    const bool fits = ex + c <= cap || lane == 0;
     nb = __popc(__ballot_sync(0xffffffffu, fits));  // counts are >= 0: a prefix of lanes
-    NearInfo mine = in;
-    if (lane >= nb) mine.cnt = 0;
-    return stage_batch<SPLIT>(sm, 0, mine, lane, src, gchi, gclo);
+    const int cnt = lane < nb ? c : 0;
+    const int staged = __shfl_sync(0xffffffffu, ex + cnt, nb - 1);
+    stage_batch<SPLIT>(sm, start, cnt, ex, staged, lane, src);
+    return staged;
 }
 
-// Moves a staged batch of ns sources from their leaves' frames into the
-// group's frame: source j adds the shift of the leaf that owns its slot.
-// The iterations are independent, so their shared-memory loads overlap.
-__device__ __forceinline__ void shift_batch(EvalSmem& sm, int ns, int lane) {
-#pragma unroll 4
-    for (int j = lane; j < ns; j += 32) {
-        const float4 sh = sm.shift[0][sm.owner[j]];
-        float4 v = sm.src[0][j];
-        v.x += sh.x;
-        v.y += sh.y;
-        v.z += sh.z;
-        sm.src[0][j] = v;
+// Pairs up a landed batch of ns sources in place: slots 2k and 2k + 1
+// become {x0 x1 y0 y1}{z0 z1 m0 m1} (an odd count pads slot ns with a zero
+// mass at the group's origin, which adds nothing).  In SPLIT precision each
+// source first moves from its leaf's frame into the group's: windows of 64
+// slots, bit i of a window's mask set where a staged leaf starts at that
+// slot, so a slot's leaf rank is the leaves started before the window plus
+// the mask bits up to it, minus one.
+template <bool SPLIT>
+__device__ __forceinline__ void pair_batch(EvalSmem& sm, int ns, int lane) {
+    const float4 pad = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (SPLIT) {
+        const int nl = sm.nleaf;
+        const int f = lane < nl ? sm.first[lane] : 0x7fffffff;
+        int before = 0;
+        for (int base = 0; base < ns; base += 64) {
+            const int o = f - base;
+            const unsigned lo = __reduce_or_sync(0xffffffffu, o >= 0 && o < 32 ? 1u << o : 0u);
+            const unsigned hi = __reduce_or_sync(0xffffffffu, o >= 32 && o < 64 ? 1u << (o - 32) : 0u);
+            const unsigned long long starts = ((unsigned long long)hi << 32) | lo;
+            const int i0 = 2 * lane, j0 = base + i0;
+            if (j0 < ns) {
+                const int l0 = before + __popcll(starts & (~0ull >> (63 - i0))) - 1;
+                const int l1 = l0 + (int)((starts >> (i0 + 1)) & 1ull);
+                const bool two = j0 + 1 < ns;
+                float4 a = sm.src[j0];
+                float4 b = two ? sm.src[j0 + 1] : pad;
+                const float4 sa = sm.shift[l0];
+                a.x += sa.x;
+                a.y += sa.y;
+                a.z += sa.z;
+                if (two) {
+                    const float4 sb = sm.shift[l1];
+                    b.x += sb.x;
+                    b.y += sb.y;
+                    b.z += sb.z;
+                }
+                sm.src[j0] = make_float4(a.x, b.x, a.y, b.y);
+                sm.src[j0 + 1] = make_float4(a.z, b.z, a.w, b.w);
+            }
+            before += __popc(lo) + __popc(hi);
+        }
+    } else {
+        for (int j0 = 2 * lane; j0 < ns; j0 += 64) {
+            const float4 a = sm.src[j0];
+            const float4 b = j0 + 1 < ns ? sm.src[j0 + 1] : pad;
+            sm.src[j0] = make_float4(a.x, b.x, a.y, b.y);
+            sm.src[j0 + 1] = make_float4(a.z, b.z, a.w, b.w);
+        }
     }
 }
 
@@ -488,7 +617,7 @@ __device__ __forceinline__ void finish_targets(EvalSmem& sm, const Lane& g, int 
 }
 
 template <bool SPLIT, bool QUAD, int SOFT>
-__global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Counters* C,
+__global__ void __launch_bounds__(kEvalThreads, kEvalMinBlocks) eval_kernel(NodeArrays T, Counters* C,
                                                             const float4* __restrict__ src,
                                                             float4* __restrict__ acc, float4* __restrict__ vel,
                                                             float4* __restrict__ vlo,
@@ -499,17 +628,16 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
     EvalSmem& sm = reinterpret_cast<EvalSmem*>(eval_smem_raw)[threadIdx.x >> 5];
     if (C->status & kStFatal) return;
     if (lane == 0) {
-        mbar_init(&sm.bar[0]);
-        mbar_init(&sm.bar[1]);
+        mbar_init(&sm.bar);
+        sm.npairs = sm.nterms = 0ull;
     }
     __syncwarp();
-    unsigned phase[2] = {0u, 0u};
+    unsigned phase = 0u;
     const int nleaves = C->nleaves;
     // Sources per near batch: the tuned cap (at most one staging buffer).
     const int maxleaf = max(1, C->max_leaf_count);
     const int tile = wp.p2p_tile > 0 && wp.p2p_tile < kSrcCap ? wp.p2p_tile : kSrcCap;
     const bool big_leaves = maxleaf > kSrcCap;
-    unsigned long long pairs = 0, p2c = 0;
     bool timeout = false;
 
     for (;;) {
@@ -523,10 +651,13 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
         const int gcount = __float_as_int(gC.w) & 0xFFFFFF;
         const int4 gin = LB.ginfo[gi];
         const int far_first = gin.x, near_first = gin.y, nfar = gin.z, nnear = gin.w;
-        float4 gchi = make_float4(0.f, 0.f, 0.f, 0.f), gclo = gchi;
         if (SPLIT) {
-            gchi = T.chi[leaf];
-            gclo = T.clo[leaf];
+            __syncwarp();
+            if (lane == 0) {
+                sm.gch = T.chi[leaf];
+                sm.gcl = T.clo[leaf];
+            }
+            __syncwarp();
         }
         for (int t0 = 0; t0 < gcount; t0 += kBlockTargets) {
             const int nblk = min(kBlockTargets, gcount - t0);
@@ -552,33 +683,20 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
             int fid = 32 + lane < nfar ? LB.far[(long long)fcur * kListChunk + 32 + lane] : -1;  // batch 1
             int nb = 0, ns_cur = 0;
             NearWindow W = {0, -1, -1, -1, -1};
-            NearInfo info;
             if (!big_leaves) {
                 W = near_window(LB, near_first, nnear, lane);
-                info = near_info_of<SPLIT>(T, W.w0);
+                prefetch_near<SPLIT>(sm, T, W.w0, lane);
             }
             Lane g = make_lane(src, gstart + t0, b0, lane);
             if (two) save_pass(sm, make_lane(src, gstart + t0 + b0, nblk - b0, lane), lane);
             if (!big_leaves) {
-                ns_cur = stage_fitting<SPLIT>(sm, info, lane, src, tile, nb, gchi, gclo);
+                ns_cur = stage_fitting<SPLIT>(sm, lane, src, tile, nb);
                 near_advance(LB, W, nb, nnear, lane);
             }
 
             // ---- far field ----
             for (int b = 0, k = 0; b < nfar; b += 32, ++k) {
-                if (b + lane < nfar) {
-                    float4 rA = A;
-                    if (SPLIT) {
-                        rA.x = (A.x - gchi.x) + (D.x - gclo.x);
-                        rA.y = (A.y - gchi.y) + (D.y - gclo.y);
-                        rA.z = (A.z - gchi.z) + (D.z - gclo.z);
-                    }
-                    sm.farA[lane] = rA;
-                    if (QUAD) {
-                        sm.farB[lane] = B;
-                        sm.farQ[lane] = make_float2(D.w, -(B.x + B.y));
-                    }
-                }
+                stage_far<SPLIT, QUAD>(sm, lane, b + lane < nfar, A, B, D);
                 __syncwarp();
                 if (fid >= 0) {  // records of batch k+1
                     A = T.wA[fid];
@@ -594,47 +712,43 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
                     }
                     if (e2 + lane < nfar) fid = LB.far[(long long)fcur * kListChunk + (e2 & (kListChunk - 1)) + lane];
                 }
-                const int nrec = min(32, nfar - b);
-                for_passes(g, two, sm, lane, [&](Lane& x) {
-                    p2c_chunk<SPLIT, QUAD, SOFT>(x, sm.farA, sm.farB, sm.farQ, nrec, wp.eps2, wp.ih);
-                });
+                const int npr = (min(32, nfar - b) + 1) >> 1;
+                for_passes(g, two, sm, lane,
+                           [&](Lane& x) { p2c_chunk<SPLIT, QUAD, SOFT>(x, sm, npr, wp.eps2, wp.ih); });
                 __syncwarp();
             }
-            p2c += (unsigned long long)nblk * (unsigned long long)nfar;
+            if (lane == 0) sm.nterms += (unsigned long long)nblk * (unsigned long long)nfar;
 
             // ---- near field: batches of up to 32 leaves (as many as fit the
             // staging buffer, by their actual counts) staged by TMA ----
             int total = 0;
             if (!big_leaves) {
                 // batch 0 was staged before the far field
-                if (W.pos < nnear) info = near_info_of<SPLIT>(T, W.w0);
+                if (W.pos < nnear) prefetch_near<SPLIT>(sm, T, W.w0, lane);
                 while (ns_cur > 0) {
-                    if (!mbar_wait(&sm.bar[0], phase[0])) {
+                    if (!mbar_wait(&sm.bar, phase)) {
                         timeout = true;
                         break;
                     }
-                    phase[0] ^= 1u;
-                    if (SPLIT) shift_batch(sm, ns_cur, lane);  // into the group's frame
+                    phase ^= 1u;
+                    pair_batch<SPLIT>(sm, ns_cur, lane);  // source pairs, in the group's frame
                     __syncwarp();
+                    const int np = (ns_cur + 1) >> 1;
                     for_passes(g, two, sm, lane,
-                               [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src[0], ns_cur, wp.eps2, wp.ih); });
+                               [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src, np, wp.eps2, wp.ih); });
                     __syncwarp();
                     total += ns_cur;
                     // stage the next batch (its info is in registers), then fetch
                     // the info of the one after
                     int ns_next = 0;
                     if (W.pos < nnear) {
-                        ns_next = stage_fitting<SPLIT>(sm, info, lane, src, tile, nb, gchi, gclo);
+                        ns_next = stage_fitting<SPLIT>(sm, lane, src, tile, nb);
                         near_advance(LB, W, nb, nnear, lane);
-                        if (W.pos < nnear) info = near_info_of<SPLIT>(T, W.w0);
+                        if (W.pos < nnear) prefetch_near<SPLIT>(sm, T, W.w0, lane);
                     }
                     ns_cur = ns_next;
                 }
-                if (timeout) {
-                    // give copies still in flight a bounded chance to land
-                    mbar_wait(&sm.bar[0], phase[0]);
-                    if (kBuffers == 2) mbar_wait(&sm.bar[1], phase[1]);
-                }
+                if (timeout) mbar_wait(&sm.bar, phase);  // give copies in flight a bounded chance to land
             } else {
                 // Leaves larger than a staging buffer (depth-limited): plain loads, piecewise.
                 int c = near_first;
@@ -645,30 +759,36 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
                     const int st = __float_as_int(Cw.z), cn = __float_as_int(Cw.w) & 0xFFFFFF;
                     float4 sh = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (SPLIT) {
-                        const float4 h = T.chi[node], l = T.clo[node];
-                        sh = make_float4((h.x - gchi.x) + (l.x - gclo.x), (h.y - gchi.y) + (l.y - gclo.y),
-                                         (h.z - gchi.z) + (l.z - gclo.z), 0.f);
+                        const float4 h = T.chi[node], l = T.clo[node], gh = sm.gch, gl = sm.gcl;
+                        sh = make_float4((h.x - gh.x) + (l.x - gl.x), (h.y - gh.y) + (l.y - gl.y),
+                                         (h.z - gh.z) + (l.z - gl.z), 0.f);
                     }
                     for (int off = 0; off < cn; off += kSrcCap) {
                         const int ns = min(kSrcCap, cn - off);
                         __syncwarp();
-                        for (int j = lane; j < ns; j += 32) {
-                            float4 v = src[st + off + j];
-                            v.x += sh.x;
-                            v.y += sh.y;
-                            v.z += sh.z;
-                            sm.src[0][j] = v;
+                        for (int j0 = 2 * lane; j0 < ns; j0 += 64) {  // pairs, in the group's frame
+                            float4 a = src[st + off + j0];
+                            float4 c = j0 + 1 < ns ? src[st + off + j0 + 1] : make_float4(-sh.x, -sh.y, -sh.z, 0.f);
+                            a.x += sh.x;
+                            a.y += sh.y;
+                            a.z += sh.z;
+                            c.x += sh.x;
+                            c.y += sh.y;
+                            c.z += sh.z;
+                            sm.src[j0] = make_float4(a.x, c.x, a.y, c.y);
+                            sm.src[j0 + 1] = make_float4(a.z, c.z, a.w, c.w);
                         }
                         __syncwarp();
+                        const int np = (ns + 1) >> 1;
                         for_passes(g, two, sm, lane,
-                                   [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src[0], ns, wp.eps2, wp.ih); });
+                                   [&](Lane& x) { p2p_chunk<SPLIT, SOFT>(x, sm.src, np, wp.eps2, wp.ih); });
                     }
                     __syncwarp();
                     total += cn;
                 }
             }
             if (timeout) break;
-            pairs += (unsigned long long)nblk * (unsigned long long)total - (unsigned long long)nblk;
+            if (lane == 0) sm.npairs += (unsigned long long)nblk * (unsigned long long)total - (unsigned long long)nblk;
 
             // ---- sum the slices of each target, write a, closing kick ----
             finish_targets<SPLIT>(sm, g, gstart + t0, lane, wp, acc, vel, vlo);
@@ -679,8 +799,8 @@ __global__ void __launch_bounds__(kEvalThreads, 6) eval_kernel(NodeArrays T, Cou
     }
     if (timeout && lane == 0) atomicOr(&C->status, kStTimeout);
     if (lane == 0) {
-        atomicAdd(&C->p2p_pairs, pairs);
-        atomicAdd(&C->p2c_terms, p2c);
+        atomicAdd(&C->p2p_pairs, sm.npairs);
+        atomicAdd(&C->p2c_terms, sm.nterms);
     }
 }
 
