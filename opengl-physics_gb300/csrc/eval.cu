@@ -127,6 +127,7 @@ __device__ __forceinline__ int excl_scan(int v, int lane, int& total) {
 // record pairs s, s + S, s + 2S, ... of a 32-record batch.
 struct Lane {
     float tx, ty, tz;
+    float rS;                                 // 1 / S, scaled up (slice_recip)
     int sl, S, nt;
     bool active;
     float ax, ay, az, cx, cy, cz;
@@ -187,11 +188,17 @@ constexpr PassSplit make_pass_split() {
 }
 __constant__ PassSplit kPassSplit = make_pass_split();
 
+// 1 / S from the hardware reciprocal, scaled up by 2^-18 so that
+// floor(n * rS) is the exact quotient n / S for every n <= 255 (the scaled
+// error stays far below the 1 / S gap to the next integer).
+__device__ __forceinline__ float slice_recip(int S) { return __fdividef(1.f, (float)S) * 1.000003814697265625f; }
+
 // Lane map of nt <= 32 targets starting at slot `first`, sums zeroed.
 __device__ __forceinline__ Lane make_lane(const float4* __restrict__ src, int first, int nt, int lane) {
     Lane g;
     g.nt = nt;
     g.S = 32 / nt;
+    g.rS = slice_recip(g.S);
     g.active = lane < nt * g.S;
     g.sl = lane / nt;
     const float4 tp = src[first + lane % nt];
@@ -219,6 +226,7 @@ __device__ __forceinline__ Lane load_pass(const EvalSmem& sm, int lane) {
     g.tz = t.z;
     g.sl = map & 0xFF;
     g.S = (map >> 8) & 0xFF;
+    g.rS = slice_recip(g.S);
     g.nt = (map >> 16) & 0xFF;
     g.active = (map >> 24) != 0;
     g.ax = a.x;
@@ -288,7 +296,7 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s2
     if (!g.active) return;
     const float2 ntx = dup2(-g.tx), nty = dup2(-g.ty), ntz = dup2(-g.tz), e2 = dup2(eps2);
     float2 ax = dup2(0.f), ay = ax, az = ax, bx = ax, by = ax, bz = ax;
-    const int len = ((np + g.S - 1) / g.S) | 1;
+    const int len = __float2int_rz((float)(np + g.S - 1) * g.rS) | 1;  // ceil(np / S), odd
     const int b = min(np, g.sl * len);
     const float4* p = s2 + 2 * b;
     const float4* const pe = s2 + 2 * min(np, b + len);
@@ -534,49 +542,46 @@ __device__ __forceinline__ int stage_fitting(EvalSmem& sm, int lane, const float
 
 // Pairs up a landed batch of ns sources in place: slots 2k and 2k + 1
 // become {x0 x1 y0 y1}{z0 z1 m0 m1} (an odd count pads slot ns with a zero
-// mass at the group's origin, which adds nothing).  In SPLIT precision each
-// source first moves from its leaf's frame into the group's: windows of 64
-// slots, bit i of a window's mask set where a staged leaf starts at that
-// slot, so a slot's leaf rank is the leaves started before the window plus
-// the mask bits up to it, minus one.
+// mass at the group's origin, which adds nothing); lane l takes pair l of
+// each window of 64 slots.  In SPLIT precision each source first moves from
+// its leaf's frame into the group's: bit i of a window's mask is set where
+// a staged leaf starts at slot i of the window (one OR-reduction per half),
+// so a slot's leaf rank is the leaves started before the window plus the
+// mask bits up to the slot, minus one.
 template <bool SPLIT>
 __device__ __forceinline__ void pair_batch(EvalSmem& sm, int ns, int lane) {
     const float4 pad = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (SPLIT) {
-        const int nl = sm.nleaf;
-        const int f = lane < nl ? sm.first[lane] : 0x7fffffff;
-        int before = 0;
-        for (int base = 0; base < ns; base += 64) {
-            const int o = f - base;
-            const unsigned lo = __reduce_or_sync(0xffffffffu, o >= 0 && o < 32 ? 1u << o : 0u);
-            const unsigned hi = __reduce_or_sync(0xffffffffu, o >= 32 && o < 64 ? 1u << (o - 32) : 0u);
+    const int f = SPLIT && lane < sm.nleaf ? sm.first[lane] : 0x7fffffff;
+    const unsigned long long upto = ~0ull >> (63 - 2 * lane);  // mask bits 0 .. 2 lane
+    int before = -1;
+#pragma unroll 2
+    for (int base = 0; base < ns; base += 64) {
+        int l0 = 0, l1 = 0;
+        if (SPLIT) {
+            const unsigned o = (unsigned)(f - base);
+            const unsigned lo = __reduce_or_sync(0xffffffffu, o < 32u ? 1u << o : 0u);
+            const unsigned hi = __reduce_or_sync(0xffffffffu, o - 32u < 32u ? 1u << (o - 32u) : 0u);
             const unsigned long long starts = ((unsigned long long)hi << 32) | lo;
-            const int i0 = 2 * lane, j0 = base + i0;
-            if (j0 < ns) {
-                const int l0 = before + __popcll(starts & (~0ull >> (63 - i0))) - 1;
-                const int l1 = l0 + (int)((starts >> (i0 + 1)) & 1ull);
-                const bool two = j0 + 1 < ns;
-                float4 a = sm.src[j0];
-                float4 b = two ? sm.src[j0 + 1] : pad;
-                const float4 sa = sm.shift[l0];
+            l0 = before + __popcll(starts & upto);
+            l1 = l0 + (int)((starts >> (2 * lane + 1)) & 1ull);
+            before += __popc(lo) + __popc(hi);
+        }
+        const int j0 = base + 2 * lane;
+        if (j0 < ns) {
+            const bool two = j0 + 1 < ns;
+            float4 a = sm.src[j0];
+            float4 b = two ? sm.src[j0 + 1] : pad;
+            if (SPLIT) {
+                const float4 sa = sm.shift[l0], sb = sm.shift[l1];
                 a.x += sa.x;
                 a.y += sa.y;
                 a.z += sa.z;
                 if (two) {
-                    const float4 sb = sm.shift[l1];
                     b.x += sb.x;
                     b.y += sb.y;
                     b.z += sb.z;
                 }
-                sm.src[j0] = make_float4(a.x, b.x, a.y, b.y);
-                sm.src[j0 + 1] = make_float4(a.z, b.z, a.w, b.w);
             }
-            before += __popc(lo) + __popc(hi);
-        }
-    } else {
-        for (int j0 = 2 * lane; j0 < ns; j0 += 64) {
-            const float4 a = sm.src[j0];
-            const float4 b = j0 + 1 < ns ? sm.src[j0 + 1] : pad;
             sm.src[j0] = make_float4(a.x, b.x, a.y, b.y);
             sm.src[j0 + 1] = make_float4(a.z, b.z, a.w, b.w);
         }
