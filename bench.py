@@ -239,11 +239,13 @@ def precision_run(pkg, ic, dev, steps=100):
     return out
 
 
-def collapse_run(pkg, ic, dev, steps=200, every=20, model=None, budget=3.5e-4, energy=False, n=16777216):
+def collapse_run(pkg, ic, dev, steps=200, every=20, model=None, budget=None, energy=False, n=16777216):
     """C5: cold collapse of a uniform ball, N = 16,777,216 (cube rejection,
     seed 4), at rest, G = 1, eps 0.001, KDK dt 1e-4 for `steps` steps with the
-    learned opening test (trained on this run unless a model is given),
-    split precision, walk stack tuned, CUDA-graph steps.  Every `every`
+    learned opening test (trained on this run unless a model is given; its
+    budget, unless given, calibrated on the initial state to the largest
+    grid value whose rms error stays within 0.95 x 1e-3, the margin for the
+    error's growth during the run), split precision, CUDA-graph steps.  Every `every`
     steps: the rms / max force error against the direct sum (FP32 pairs,
     FP64 sums) on 4,096 targets, the leaves at the 21-level key limit, and
     |L|; energy (exact pair potential, FP32 pair terms, about a minute at
@@ -266,7 +268,27 @@ def collapse_run(pkg, ic, dev, steps=200, every=20, model=None, budget=3.5e-4, e
         rec["train_wall_s"] = time.perf_counter() - t0
         sim.lmac_set_model(*model)
         sim.set_opts(mac=pkg.MAC_LEARNED)
-        sim.lmac_set_opts(budget=budget, check_every=10, check_targets=CHECK_TARGETS, revert_rms=1.5e-3)
+        screen = None
+        if budget is None:
+            # the screen factor too: the relative error near the ball's centre,
+            # where |a| -> 0, is more sensitive to the error bound's slack
+            best = None
+            for scr in (1000.0, 300.0):
+                def set_budget(v, scr=scr):
+                    sim.lmac_set_opts(budget=v, check_every=0, screen=scr)
+                b, tab = calibrate(sim, COLLAPSE_BUDGET_GRID, set_budget, target=0.95 * TARGET_RMS, stop=1.3)
+                set_budget(b)
+                ms = []
+                for _ in range(3):
+                    sim.compute_accel()
+                    ms.append(sum(phases(sim.stats()).values()))
+                ms = min(ms)
+                if best is None or ms < best[0]:
+                    best = (ms, scr, b, tab)
+            _, screen, budget, rec["calibration"] = best
+            rec["budget"], rec["screen"] = budget, screen
+        kw = {} if screen is None else {"screen": screen}
+        sim.lmac_set_opts(budget=budget, check_every=10, check_targets=CHECK_TARGETS, revert_rms=1.5e-3, **kw)
         sim.prime()
         d0 = sim.diagnostics(exact_potential=2 if energy else 0)
         ms = 0.0
@@ -389,9 +411,12 @@ def run_reference(args, rank, world):
     return 0
 
 
-THETA_GRID = (0.5, 0.55, 0.575, 0.6, 0.6125, 0.625, 0.6375, 0.65, 0.6625, 0.675, 0.7, 0.75, 0.8)
-BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 2.75e-4, 3e-4, 3.25e-4, 3.5e-4, 3.75e-4, 4e-4, 4.5e-4, 5e-4,
-               7e-4, 1e-3)
+THETA_GRID = (0.5, 0.55, 0.575, 0.6, 0.605, 0.61, 0.615, 0.62, 0.625, 0.63, 0.635, 0.64, 0.645, 0.65, 0.6625,
+              0.675, 0.7, 0.75, 0.8)
+# budgets ~12 % apart from 2e-5 to 1e-3 (the cold collapse's calibration)
+COLLAPSE_BUDGET_GRID = tuple(float("%.3g" % (2e-5 * 1.12 ** k)) for k in range(35))
+BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 2.75e-4, 3e-4, 3.1e-4, 3.2e-4, 3.3e-4, 3.4e-4, 3.5e-4, 3.6e-4,
+               3.7e-4, 3.8e-4, 3.9e-4, 4e-4, 4.5e-4, 5e-4, 7e-4, 1e-3)
 TARGET_RMS = 1e-3
 # The learned test's in-run safety check: every 10 steps an FP64-summed
 # direct sum on this many sampled targets judges the rms error (about +-3 %
@@ -407,8 +432,10 @@ def error_at(sim, seed=2024):
     return sim.force_error(nsample=4096, seed=seed, fp64_pairs=False)
 
 
-def calibrate(sim, grid, setter, target=TARGET_RMS):
-    """Largest grid value whose rms error stays within the target."""
+def calibrate(sim, grid, setter, target=TARGET_RMS, stop=None):
+    """Largest grid value whose rms error stays within the target (the grid
+    ascends in error; with `stop`, the scan ends once the rms passes stop x
+    the target)."""
     table, best = [], None
     for v in grid:
         setter(v)
@@ -416,6 +443,8 @@ def calibrate(sim, grid, setter, target=TARGET_RMS):
         table.append([v, fe["rms"], fe["max"]])
         if fe["rms"] <= target:
             best = v
+        elif stop and fe["rms"] > stop * target:
+            break
     return (best if best is not None else grid[0]), table
 
 
@@ -813,7 +842,7 @@ def main():
         extra = {}
         for name, fn in (("C2_plummer1m_precision", lambda: precision_run(pkg, ic, dev, steps=100)),
                          ("C3_ensemble512", lambda: ensemble_run(pkg, ic, dev, steps=10, warmup=3, tune_reps=1)),
-                         ("C5_collapse16m", lambda: collapse_run(pkg, ic, dev, budget=budget or 3.5e-4))):
+                         ("C5_collapse16m", lambda: collapse_run(pkg, ic, dev))):
             t0 = time.perf_counter()
             try:
                 extra[name] = fn()

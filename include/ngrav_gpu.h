@@ -381,7 +381,7 @@ typedef struct ngrav_gpu_lmac_opts {
                             * truncation bound on its error is at most screen x budget x
                             * the group's smallest |a| (0: every band pair goes to the
                             * network); the bound is loose by orders of magnitude, hence
-                            * the default 300 */
+                            * the default 1000 */
 } ngrav_gpu_lmac_opts;
 
 typedef struct ngrav_gpu_lmac_train_opts {

@@ -422,14 +422,14 @@ int ngrav_gpu_lmac_default_opts(ngrav_gpu_lmac_opts* o) {
     if (!o) return NGRAV_ERR_INVALID_ARG;
     std::memset(o, 0, sizeof(*o));
     o->budget = 3e-5;
-    o->gate = 2.0;
+    o->gate = 0.25;
     o->rho_lo = 0.25;
     o->rho_hi = 1.25;
     o->check_every = 10;
     o->check_targets = 4096;
     o->revert_rms = 1e-3;
     o->rounds = 3;
-    o->screen = 300.0;
+    o->screen = 1000.0;
     return NGRAV_OK;
 }
 
