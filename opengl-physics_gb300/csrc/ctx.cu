@@ -214,13 +214,19 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     ctx->launches += launch_keys(P.pos, split ? P.plo : nullptr, n, ctx->C, ctx->F, ctx->SB.ktab, ctx->SB.keys,
                                  ctx->SB.vals, s) - 1;
     rec(ctx, 1);
-    const int passes = kRsPasses;
-    radix_sort_pairs(ctx->SB, n, passes, s);
+    // The keys are sorted on their top `levels` digits only (whole 9-bit
+    // passes, so at least that many levels), as deep as the tree went at the
+    // last evaluation plus a level; a node at the deepest sorted level that
+    // would still split stops the build (kStSortDepth) and the evaluation
+    // is redone on the full key.
+    const int levels = ctx->F.nsys > 1 ? kKeyLevels : ctx->sort_levels;
+    const int passes = std::min(kRsPasses, (3 * levels + kRsDigitBits - 1) / kRsDigitBits);
+    radix_sort_pairs(ctx->SB, n, passes, 3 * kKeyLevels - kRsDigitBits * passes, s);
     launch_permute(P, ctx->SB.vals, n, split, s);
     // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,
-    // tree init, 21 levels, leaf list (mark, 3 scan kernels, compact), leaf
-    // moments, 21 internal-moment levels, walk
-    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + kKeyLevels + 5 + 1 + kKeyLevels + 1;
+    // tree init, the levels, leaf list (mark, 3 scan kernels, compact), leaf
+    // moments, the internal-moment levels, walk
+    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + levels + 5 + 1 + levels + 1;
     std::swap(P.pos, P.pos2);
     std::swap(P.plo, P.plo2);
     std::swap(P.vel, P.vel2);
@@ -229,11 +235,12 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     std::swap(P.id, P.id2);
     rec(ctx, 2);
     launch_tree_init(ctx->T, ctx->C, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, s);
-    launch_tree_levels(ctx->T, ctx->C, ctx->SB.keys, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, ctx->F, s);
+    launch_tree_levels(ctx->T, ctx->C, ctx->SB.keys, n, ctx->opts.leaf_capacity, ctx->opts.max_depth, ctx->F, levels,
+                       s);
     launch_leaf_list(ctx->T, ctx->C, n, ctx->leaf_at, ctx->flags, ctx->scanbuf, ctx->leaf_list, ctx->SB, s);
     rec(ctx, 3);
     launch_moments(ctx->T, ctx->C, P, ctx->leaf_list, n, (int)std::min<long long>(n, ctx->T.cap), split,
-                   ctx->opts.quadrupole != 0, s);
+                   ctx->opts.quadrupole != 0, levels, s);
     rec(ctx, 4);
     WalkParams wp = walk_params(ctx, kick, hdt);
     const void* model = nullptr;
@@ -270,6 +277,11 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
         const long long want = std::min<long long>((long long)ctx->T.cap * 2, 0x7FFFFFF0LL);
         if (want <= ctx->T.cap) return fail(ctx, NGRAV_ERR_CAPACITY, "node pool exhausted");
         NG_TRY(alloc_nodes(ctx, (int)want));
+        retry = true;
+        return NGRAV_OK;
+    }
+    if (st & kStSortDepth) {
+        ctx->sort_levels = kKeyLevels;  // the tree went deeper than the sorted digits
         retry = true;
         return NGRAV_OK;
     }
@@ -319,6 +331,13 @@ int finish_eval(ngrav_gpu_ctx* ctx, bool& retry) {
         ctx->cum_ms_eval += ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] +
                             ctx->phase_ms[4] + ctx->phase_ms[5];
     }
+    {
+        // sort and build one level deeper than this tree next time; shrink only
+        // when the tree is two levels shallower, so a depth that wavers by one
+        // level does not re-capture the step graph
+        const int want = std::min(kKeyLevels, std::max(1, ctx->hc.levels_used + 1));
+        if (want > ctx->sort_levels || want + 1 < ctx->sort_levels) ctx->sort_levels = want + (want < ctx->sort_levels);
+    }
     ctx->force_evals += 1;
     ctx->cum_particle_evals += ctx->block_on ? (long long)ctx->hc.targets : ctx->n;
     ctx->acc_valid = true;
@@ -366,6 +385,7 @@ int set_particles_impl(ngrav_gpu_ctx* ctx, int64_t n, const T* x, const T* y, co
                        const T* vz, const T* m, bool f64) {
     if (n < 0 || n > 0x7FFFFFF0LL) return fail(ctx, NGRAV_ERR_INVALID_ARG, "n out of range");
     if (n > 0 && (!x || !y || !z || !m)) return fail(ctx, NGRAV_ERR_INVALID_ARG, "NULL position/mass array");
+    ctx->sort_levels = kKeyLevels;  // a new particle set: sort and build on the full key once
     const bool have_v = vx && vy && vz;
     NG_CUDA(cudaSetDevice(ctx->opts.device));
     NG_TRY(alloc_particles(ctx, std::max<int64_t>(n, 1)));
@@ -436,6 +456,7 @@ std::vector<unsigned char> step_key(const ngrav_gpu_ctx* ctx, float hdt, float f
     put(&ctx->soft, sizeof(ctx->soft));
     put(&ctx->alpha, sizeof(ctx->alpha));
     put(&ctx->p2p_tile, sizeof(ctx->p2p_tile));
+    put(&ctx->sort_levels, sizeof(ctx->sort_levels));
     put(&ctx->events, sizeof(ctx->events));
     put(&hdt, sizeof(hdt));
     put(&fdt, sizeof(fdt));
@@ -651,6 +672,8 @@ int ngrav_gpu_set_opts(ngrav_gpu_ctx* ctx, const ngrav_gpu_opts* opts) {
         }
         NG_CUDA(cudaStreamSynchronize(ctx->stream));
     }
+    if (opts->leaf_capacity != ctx->opts.leaf_capacity || opts->max_depth != ctx->opts.max_depth)
+        ctx->sort_levels = kKeyLevels;  // another tree: sort and build on the full key once
     ctx->opts = *opts;
     ctx->events = ctx->opts.timing != 0;
     ctx->primed = false;

@@ -39,8 +39,9 @@ enum : unsigned {
     kStListOverflow = 32u,  // per-warp list staging or the final list pool
     kStCorrupt = 64u,       // walk visit limit breached
     kStPendOverflow = 128u, // learned walk: deferred-pair pool exhausted
+    kStSortDepth = 256u,    // a node at the deepest sorted key level still needs splitting
     kStFatal = kStNodeOverflow | kStStackOverflow | kStNonFinite | kStTimeout | kStListOverflow | kStCorrupt |
-               kStPendOverflow,
+               kStPendOverflow | kStSortDepth,
 };
 
 // Per-evaluation device counters (zeroed before each force evaluation).
@@ -258,17 +259,19 @@ void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s
 // the centre table ktab (3 * kKeyTabSize doubles).  Returns the launches made.
 int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
-// Stable LSD radix sort of (keys, vals) over bits [0, kRsDigitBits*passes); result ends
-// in (keys, vals) (the alternates are scratch).
-void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s);
+// Stable LSD radix sort of (keys, vals) over bits [shift0, shift0 + kRsDigitBits*passes);
+// result ends in (keys, vals) (the alternates are scratch).
+void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cudaStream_t s);
 void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);
 void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s);
+// Builds levels 1 .. levels (keys sorted on their top `levels` digits); a node
+// at level `levels` that would still split sets kStSortDepth.
 void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
-                        int max_depth, const Forest& F, cudaStream_t s);
+                        int max_depth, const Forest& F, int levels, cudaStream_t s);
 void launch_leaf_list(NodeArrays& T, Counters* C, long long n, int* leaf_at, unsigned* flags, unsigned* scan_out,
                       int* leaf_list, SortBuffers& sb, cudaStream_t s);
 void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,
-                    int max_leaves, bool split, bool quadrupole, cudaStream_t s);
+                    int max_leaves, bool split, bool quadrupole, int levels, cudaStream_t s);
 void launch_walk(const NodeArrays& T, Counters* C, const int* leaf_list, const WalkParams& wp,
                  const ListBuffers& LB, cudaStream_t s);
 void launch_eval(const NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, const WalkParams& wp,

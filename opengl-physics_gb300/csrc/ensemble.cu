@@ -231,6 +231,7 @@ int ngrav_gpu_set_ensemble(ngrav_gpu_ctx* ctx, int nsys, const int64_t* offsets)
     if (levels > 6) return fail(ctx, NGRAV_ERR_INVALID_ARG, "at most 8^6 systems");
     NG_CUDA(cudaSetDevice(ctx->opts.device));
     free_forest(ctx);
+    ctx->sort_levels = kKeyLevels;  // another tree: sort and build on the full key once
     if (nsys == 1) return NGRAV_OK;  // one system: the plain tree
     NG_CUDA(dalloc(ctx->f_off, nsys + 1));
     NG_CUDA(dalloc(ctx->f_root, 4LL * nsys));

@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
     }
 }
 
-void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s) {
+void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cudaStream_t s) {
     if (n <= 1) return;
     const int nb = (int)((n + kRsTile - 1) / kRsTile);
     const size_t smem = (size_t)kRsTile * (sizeof(unsigned long long) + sizeof(unsigned));
@@ -598,7 +598,7 @@ void radix_sort_pairs(SortBuffers& sb, long long n, int passes, cudaStream_t s) 
     unsigned* vin = sb.vals;
     unsigned* vout = sb.vals_alt;
     for (int p = 0; p < passes; ++p) {
-        const int shift = kRsDigitBits * p;
+        const int shift = shift0 + kRsDigitBits * p;
         rs_hist_kernel<<<nb, kRsThreads, 0, s>>>(kin, n, shift, sb.hist);
         device_exclusive_scan(sb.hist, sb.hist, (long long)nb * kRsBins, sb.scan_tmp, s);
         rs_scatter_kernel<<<nb, kRsThreads, smem, s>>>(kin, vin, kout, vout, n, shift, sb.hist);

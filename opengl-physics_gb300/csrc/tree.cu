@@ -79,7 +79,8 @@ constexpr int kLevelThreads = 256;
 // the reference's recurrence runs from that root.
 __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T, Counters* C,
                                                                    const unsigned long long* __restrict__ keys,
-                                                                   int l, int leaf_cap, int max_depth, Forest F) {
+                                                                   int l, int leaf_cap, int max_depth, Forest F,
+                                                                   int levels) {
     const int begin = C->level_begin[l];
     const int end = C->level_begin[l + 1];
     const int shift = 3 * (kKeyLevels - 1 - l);
@@ -175,6 +176,11 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
             if (l + 1 >= kKeyLevels && ce - cs > leaf_cap && l + 1 < depth_cap) {
                 atomicOr(&C->status, kStDepthLimit);
                 atomicAdd(&C->depth_limited, 1);
+            } else if (l + 1 == levels && ce - cs > leaf_cap && l + 1 < depth_cap) {
+                // the keys were sorted on `levels` digits only: this child
+                // would split on an unsorted digit, so the build is redone on
+                // the full key
+                atomicOr(&C->status, kStSortDepth);
             }
         }
         if (d == 0) {
@@ -198,14 +204,14 @@ __global__ void __launch_bounds__(kLevelThreads) tree_level_kernel(NodeArrays T,
 }
 
 void launch_tree_levels(NodeArrays& T, Counters* C, const unsigned long long* keys, long long n, int leaf_cap,
-                        int max_depth, const Forest& F, cudaStream_t s) {
+                        int max_depth, const Forest& F, int levels, cudaStream_t s) {
     // Enough threads for the widest level (nodes <= cap); levels above it
     // exit after a bounds check.
     long long blocks = ((long long)T.cap / 4 * 8 + kLevelThreads - 1) / kLevelThreads;
     if (blocks > 152 * 8) blocks = 152 * 8;
     if (blocks < 1) blocks = 1;
-    for (int l = 0; l < kKeyLevels; ++l)
-        tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth, F);
+    for (int l = 0; l < levels; ++l)
+        tree_level_kernel<<<(unsigned)blocks, kLevelThreads, 0, s>>>(T, C, keys, l, leaf_cap, max_depth, F, levels);
 }
 
 // ---------------------------------------------------------------------------
@@ -508,7 +514,7 @@ __global__ void __launch_bounds__(256) internal_moments_kernel(NodeArrays T, con
 }
 
 void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* leaf_list, long long n,
-                    int max_leaves, bool split, bool quadrupole, cudaStream_t s) {
+                    int max_leaves, bool split, bool quadrupole, int levels, cudaStream_t s) {
     long long blocks = ((long long)max_leaves + 127) / 128;
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
@@ -517,7 +523,7 @@ void launch_moments(NodeArrays& T, Counters* C, const Particles& P, const int* l
     long long b2 = ((long long)T.cap / 4 + 255) / 256;
     if (b2 > 152 * 4) b2 = 152 * 4;
     if (b2 < 1) b2 = 1;
-    for (int l = kKeyLevels - 1; l >= 0; --l)
+    for (int l = levels - 1; l >= 0; --l)
         internal_moments_kernel<<<(unsigned)b2, 256, 0, s>>>(T, C, l, quadrupole ? 1 : 0);
 }
 

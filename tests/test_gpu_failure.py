@@ -12,12 +12,16 @@ the host reads after each evaluation:
   evaluation re-runs, also inside a graph-captured KDK step; the states are
   bit-identical to a run that never overflowed;
 - the learned walk's deferred-pair pool overflows the same way, and the
-  re-run evaluation still counts toward the FP64 check cadence.
+  re-run evaluation still counts toward the FP64 check cadence;
+- the keys are sorted only as deep as the last tree went (plus a level);
+  a tree that suddenly goes deeper stops its build (a node at the deepest
+  sorted level would still split) and the evaluation re-runs on the full
+  key, with the same tree and accelerations as a fresh context.
 """
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import TREE_EXACT, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -119,3 +123,44 @@ def test_learned_pool_overflow_reruns_and_keeps_check_cadence(pkg, ic):
     # one FP64 check per learned evaluation, the re-run one included
     assert st1["lmac_checks"] == st0["lmac_checks"]
     assert st1["cum_launches"] > st0["cum_launches"]
+
+
+def test_tree_deeper_than_the_sorted_key_levels_rebuilds_on_the_full_key(pkg):
+    d = load_golden("plummer16k.npz")
+    x, y, z = (np.array(d[k], dtype=np.float64) for k in ("x", "y", "z"))
+    vx, vy, vz = (np.array(d[k], dtype=np.float64) for k in ("vx", "vy", "vz"))
+    # 400 particles pulled into a cube of half-size 1e-3 around particle 0:
+    # the tree there needs several more levels than the sphere's (and still
+    # far fewer than 21, so every key stays distinct)
+    rng = np.random.default_rng(7)
+    idx = rng.choice(np.arange(1, len(x)), size=400, replace=False)
+    x2, y2, z2 = x.copy(), y.copy(), z.copy()
+    for a, b in ((x2, x), (y2, y), (z2, z)):
+        a[idx] = b[0] + 1e-3 * rng.uniform(-1, 1, idx.size)
+    with golden_sim(pkg, d) as sim:
+        sim.compute_accel()
+        shallow = sim.stats()["levels"]
+        sim.compute_accel()  # sorted to the shallow tree's depth from here on
+        launches0 = sim.stats()["cum_launches"]
+        sim.compute_accel()
+        launches1 = sim.stats()["cum_launches"] - launches0
+        sim.set_state(x2, y2, z2, vx, vy, vz)
+        sim.reset_cumulative()
+        a1 = sim.compute_accel()
+        st1 = sim.stats()
+        t1 = sim.debug_tree()
+    with golden_sim(pkg, d) as fresh:
+        fresh.set_particles(x2, y2, z2, vx, vy, vz, d["m"])
+        a0 = fresh.compute_accel()
+        st0 = fresh.stats()
+        t0 = fresh.debug_tree()
+    assert st1["levels"] > shallow + 1  # deeper than the sorted levels: the build was redone
+    assert st1["cum_launches"] > launches1  # one evaluation, two builds
+    assert st1["status_bits"] & 0x1FF == 0 and st1["levels"] == st0["levels"]
+    assert np.array_equal(t1["order"], t0["order"])
+    c1, c0 = pkg.canonical(t1), pkg.canonical(t0)
+    for k in TREE_EXACT:
+        assert np.array_equal(c1[k], c0[k]), k
+    assert st1["p2p_pairs"] == st0["p2p_pairs"] and st1["p2c_terms"] == st0["p2c_terms"]
+    for u, v in zip(a1, a0):
+        np.testing.assert_array_equal(u, v)
