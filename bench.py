@@ -81,11 +81,11 @@ WORKLOADS = {
 }
 # DRAM bytes (read + write) per interaction-list entry of one eval_kernel launch,
 # from dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture at
-# N = 1,048,576, leaf capacity 40, learned test (290.8 + 38.6 MB for 8.95e7
+# N = 1,048,576, leaf capacity 64, learned test (171.4 + 28.4 MB for 5.77e7
 # entries; profiles/eval_kernel_galaxy1m.txt).  The lists, the first touch of
 # the particle tiles and the closing kick are the kernel's DRAM stream, so
 # traffic scales with entries.
-EVAL_DRAM_BYTES_PER_LIST_ENTRY = 3.68
+EVAL_DRAM_BYTES_PER_LIST_ENTRY = 3.46
 METRIC = "particle-steps/s at N=4M, learned-MAC vs plain θ-MAC at equal 1e-3 rms force err"
 
 
