@@ -289,8 +289,8 @@ __device__ __forceinline__ void p2p_pair2(const float4& P, const float4& Q, floa
 // One staged chunk of np source pairs against the lane's target.  Slice s
 // takes a contiguous run of len = ceil(np / S) pairs (rounded up to odd: the
 // slices of a quarter-warp then read distinct shared-memory bank groups in
-// the same LDS.128), walked four pairs at a time with immediate offsets from
-// one pointer, in two independent accumulation chains.
+// the same LDS.128), walked eight (then four) pairs at a time with immediate
+// offsets from one pointer, in two independent accumulation chains.
 template <bool SPLIT, int SOFT>
 __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s2, int np, float eps2, float ih) {
     if (!g.active) return;
@@ -300,6 +300,18 @@ __device__ __forceinline__ void p2p_chunk(Lane& g, const float4* __restrict__ s2
     const int b = min(np, g.sl * len);
     const float4* p = s2 + 2 * b;
     const float4* const pe = s2 + 2 * min(np, b + len);
+    for (; p + 16 <= pe; p += 16) {  // eight pairs in flight
+        const float4 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3], a4 = p[4], a5 = p[5], a6 = p[6], a7 = p[7];
+        const float4 a8 = p[8], a9 = p[9], a10 = p[10], a11 = p[11], a12 = p[12], a13 = p[13], a14 = p[14], a15 = p[15];
+        p2p_pair2<SOFT>(a0, a1, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a2, a3, ntx, nty, ntz, e2, ih, bx, by, bz);
+        p2p_pair2<SOFT>(a4, a5, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a6, a7, ntx, nty, ntz, e2, ih, bx, by, bz);
+        p2p_pair2<SOFT>(a8, a9, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a10, a11, ntx, nty, ntz, e2, ih, bx, by, bz);
+        p2p_pair2<SOFT>(a12, a13, ntx, nty, ntz, e2, ih, ax, ay, az);
+        p2p_pair2<SOFT>(a14, a15, ntx, nty, ntz, e2, ih, bx, by, bz);
+    }
     for (; p + 8 <= pe; p += 8) {
         const float4 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3], a4 = p[4], a5 = p[5], a6 = p[6], a7 = p[7];
         p2p_pair2<SOFT>(a0, a1, ntx, nty, ntz, e2, ih, ax, ay, az);
