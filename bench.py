@@ -491,13 +491,20 @@ def timed(sim, steps, warmup, dt, clocks=None, dist=None, diag=None):
 def drift(d0, d1, mtot):
     """Relative conservation errors between two FP64 diagnostics: energy
     (E1 - E0) / |E0|; momentum |P1 - P0| over the momentum scale
-    sqrt(2 M K0) (the system's net momentum is ~0 in the COM frame);
-    angular momentum |L1 - L0| / |L0|."""
+    sqrt(2 M K) (the net momentum is ~0 in the COM frame; K the larger of the
+    two kinetic energies, so a cold start is measured against the motion it
+    develops); angular momentum |L1 - L0| / |L0|, or, when the system starts
+    without angular momentum (a cold collapse), over sqrt(2 M K) x one length
+    unit (the ball's radius).  The absolute changes are given too."""
     dP = float(np.linalg.norm(np.subtract(d1["P"], d0["P"])))
+    dL = float(np.linalg.norm(np.subtract(d1["L"], d0["L"])))
     L0 = float(np.linalg.norm(d0["L"]))
+    pscale = float(np.sqrt(2.0 * mtot * max(d0["kinetic"], d1["kinetic"])))
     return {"energy_drift": (d1["energy"] - d0["energy"]) / abs(d0["energy"]),
-            "momentum_drift": dP / np.sqrt(2.0 * mtot * d0["kinetic"]),
-            "angular_momentum_drift": float(np.linalg.norm(np.subtract(d1["L"], d0["L"]))) / L0 if L0 > 0 else None,
+            "momentum_drift": dP / pscale if pscale > 0 else None, "momentum_change": dP,
+            "angular_momentum_drift": dL / L0 if L0 > 0 else (dL / pscale if pscale > 0 else None),
+            "angular_momentum_change": dL,
+            "angular_momentum_scale": "|L0|" if L0 > 0 else "sqrt(2 M K) x 1 length unit (L0 = 0)",
             "potential": "exact pair sum, FP32 pair terms, FP64 sums" if d0["potential_exact"] == 2 else
                          ("exact pair sum, FP64" if d0["potential_exact"] == 1 else "none")}
 
@@ -527,42 +534,52 @@ def fp32_peak_detail(dev, probe, clk):
 
 
 def sort_roofline(st, n, split):
-    """The HBM-bound part of the tree build: the LSD radix sort (7 passes of
-    9-bit digits; each reads and writes 8 B keys + 4 B slots) and the
-    permutation of the state into key order (split: pos, plo, vel, vlo, acc
-    read and written, id moved, the permutation read), algorithmic bytes over
-    the phase's event time."""
-    per = 7 * 24 + ((5 * 16 + 4 + 4) + (5 * 16 + 4) if split else (3 * 16 + 4 + 4) + (3 * 16 + 4))
+    """The HBM-bound part of the tree build: the LSD radix sort (the
+    evaluation's passes of 9-bit digits, up to 7; each reads and writes 8 B
+    keys + 4 B slots) and the permutation of the state into key order
+    (split: pos, plo, vel, vlo, acc read and written, id moved, the
+    permutation read), algorithmic bytes over the phase's event time."""
+    passes = st.get("sort_passes", 7)
+    per = passes * 24 + ((5 * 16 + 4 + 4) + (5 * 16 + 4) if split else (3 * 16 + 4 + 4) + (3 * 16 + 4))
     ms = st["ms_sort"]
     peak, src = hbm_peak()
     ach = per * n / (ms * 1e-3) / 1e9 if ms > 0 else None
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
-            "traffic": None, "bytes_per_particle": per, "kernel": "radix sort (rs_hist, rs_scatter) + permute",
+            "traffic": None, "bytes_per_particle": per, "sort_passes": passes,
+            "kernel": "radix sort (rs_hist, rs_scatter) + permute",
             "peak_source": src}
 
 
-def p2p_phase_roofline(pkg, ic, dev, peak, prec):
+def p2p_phase_roofline(pkg, ic, dev, peak, prec, leaf_capacities=(32, 64, 128)):
     """The evaluation kernel's P2P phase on its own: a Plummer sphere of
     262,144 particles at theta = 0, where the walk opens every node, so every
     interaction is a near-field pair (no P2C term); 20 algorithmic flops per
     pair over the kernel's event time (best of three evaluations), against
-    the measured FP32 peak."""
+    the measured FP32 peak.  The headline figure is at leaf capacity 32 (a
+    mean of 9.6 targets per group); the same at larger groups shows how the
+    staging cost per source spreads over more targets."""
     arrs = ic.plummer(262144, seed=5)
-    best = None
-    with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=0.01, theta=0.0), leaf_capacity=32, precision=prec,
-                         device=dev, timing=True) as s:
-        s.set_particles_f32(*arrs)
-        for _ in range(3):
-            s.compute_accel()
-            st = s.stats()
-            if best is None or st["ms_force"] < best[0]:
-                best = (st["ms_force"], st["p2p_pairs"], st["p2c_terms"])
-    ms, pairs, terms = best
-    ach = 20.0 * pairs / (ms * 1e-3) / 1e12 if ms > 0 else None
-    return {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-            "frac": ach / peak if ach and peak else None, "kernel": "eval_kernel, P2P only (20 flops/pair)",
-            "workload": "Plummer N=262144, theta 0 (all pairs near), leaf capacity 32", "p2p_pairs": pairs,
-            "p2c_terms": terms, "ms": ms}
+    rows = {}
+    for L in leaf_capacities:
+        best = None
+        with pkg.NBodySystem(pkg.StepParams(G=1.0, eps=0.01, theta=0.0), leaf_capacity=L, precision=prec,
+                             device=dev, timing=True) as s:
+            s.set_particles_f32(*arrs)
+            for _ in range(3):
+                s.compute_accel()
+                st = s.stats()
+                if best is None or st["ms_force"] < best[0]:
+                    best = (st["ms_force"], st["p2p_pairs"], st["p2c_terms"], st["leaves"])
+        ms, pairs, terms, leaves = best
+        ach = 20.0 * pairs / (ms * 1e-3) / 1e12 if ms > 0 else None
+        rows[L] = {"achieved": ach, "frac": ach / peak if ach and peak else None, "ms": ms, "p2p_pairs": pairs,
+                   "p2c_terms": terms, "mean_group": 262144 / max(1, leaves)}
+    r = rows[leaf_capacities[0]]
+    return {"bound": "fp32", "achieved": r["achieved"], "peak": peak, "unit": "TFLOP/s", "frac": r["frac"],
+            "kernel": "eval_kernel, P2P only (20 flops/pair)",
+            "workload": f"Plummer N=262144, theta 0 (all pairs near), leaf capacity {leaf_capacities[0]}",
+            "p2p_pairs": r["p2p_pairs"], "p2c_terms": r["p2c_terms"], "ms": r["ms"],
+            "by_leaf_capacity": {str(L): v for L, v in rows.items()}}
 
 
 def phases(st):

@@ -143,6 +143,10 @@ typedef struct ngrav_gpu_stats {
      * computed, all particles per evaluation, the closing set per block-step
      * substep; cumulative */
     long long cum_particle_evals;
+    /* radix-sort passes of the last evaluation: the keys are sorted one
+     * level below the last tree's depth, in whole 9-bit passes (7 = the full
+     * 63-bit key) */
+    int sort_passes;
 } ngrav_gpu_stats;
 
 typedef struct ngrav_gpu_ctx ngrav_gpu_ctx;

@@ -95,7 +95,8 @@ class Stats(ctypes.Structure):
                 ("lmac_screened", ctypes.c_longlong),
                 ("lmac_active", ctypes.c_int), ("lmac_reverted", ctypes.c_int), ("lmac_checks", ctypes.c_int),
                 ("lmac_last_check_rms", ctypes.c_double), ("graph_captures", ctypes.c_longlong),
-                ("graph_replays", ctypes.c_longlong), ("cum_particle_evals", ctypes.c_longlong)]
+                ("graph_replays", ctypes.c_longlong), ("cum_particle_evals", ctypes.c_longlong),
+                ("sort_passes", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -222,6 +222,7 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     const int levels = ctx->F.nsys > 1 ? kKeyLevels : ctx->sort_levels;
     const int passes = std::min(kRsPasses, (3 * levels + kRsDigitBits - 1) / kRsDigitBits);
     radix_sort_pairs(ctx->SB, n, passes, 3 * kKeyLevels - kRsDigitBits * passes, s);
+    ctx->sort_passes = passes;
     launch_permute(P, ctx->SB.vals, n, split, s);
     // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,
     // tree init, the levels, leaf list (mark, 3 scan kernels, compact), leaf
@@ -1051,6 +1052,7 @@ int ngrav_gpu_get_stats(ngrav_gpu_ctx* ctx, ngrav_gpu_stats* out) {
     out->ms_build = ctx->phase_ms[2];
     out->ms_moments = ctx->phase_ms[3];
     out->cum_particle_evals = ctx->cum_particle_evals;
+    out->sort_passes = ctx->sort_passes;
     out->ms_walk = ctx->phase_ms[4];
     out->ms_force = ctx->phase_ms[5];
     out->ms_total = ctx->phase_ms[0] + ctx->phase_ms[1] + ctx->phase_ms[2] + ctx->phase_ms[3] + ctx->phase_ms[4] +

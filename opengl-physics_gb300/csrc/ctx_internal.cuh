@@ -59,6 +59,7 @@ struct ngrav_gpu_ctx {
     bool acc_valid = false;           // P.acc holds a force evaluation of this particle set
     int walk_stack = 2048;            // tuned: per-warp shared-memory walk stack entries
     int sort_levels = kKeyLevels;     // key levels sorted and built (adapted to the tree's depth)
+    int sort_passes = kRsPasses;      // radix-sort passes of the last evaluation enqueued
     int p2p_tile = 0;                 // tuned: sources per near batch (0: the kernel's maximum)
     int soft = 0;                     // kSoftPlummer / kSoftSpline (softening.cuh)
     double alpha = 0.001;             // relative opening test tolerance
