@@ -13,7 +13,7 @@ Headline: the learned opening test against the plain theta test at equal
 rms relative force error (1e-3, FP64-summed direct sum on 4,096 targets).
 Setup, untimed: for each leaf capacity of --leaf-grid (the target-group
 size), the network is trained on the run itself (16 snapshots, 2^22
-labelled pairs), and theta and the learned budget are each set to the
+labelled pairs, 8 epochs), and theta and the learned budget are each set to the
 largest grid value whose error stays within the target; each arm then runs
 at the leaf capacity whose calibrated evaluation is fastest, with the
 faster of the two walk-stack sizes.  Both arms
@@ -673,7 +673,7 @@ def main():
         if learned:
             t0 = time.perf_counter()
             row["train"] = sim.lmac_train(snapshots=args.lmac_snapshots, steps_between=1, dt=dt,
-                                          pairs=args.lmac_pairs, epochs=4, batch=8192, seed=1)
+                                          pairs=args.lmac_pairs, epochs=8, batch=8192, seed=1)
             row["train"]["wall_s"] = time.perf_counter() - t0
             row["model"] = sim.lmac_get_model()
             restart(L)  # training stepped the system: start again from the inputs
