@@ -355,9 +355,9 @@ def cpu_baseline(orc, arrs, eps, theta, ncrit, target_s=15.0):
 
 
 # The theta test's setting at the 1e-3 rms target on the galaxy (the GPU
-# theta arm calibrates to it: theta 0.625 at leaf capacity 32); the CPU arm
+# theta arm calibrates to it: theta 0.63 at leaf capacity 40); the CPU arm
 # runs the reference's algorithm at that setting and states its own error.
-REF_THETA, REF_LEAF = 0.625, 32
+REF_THETA, REF_LEAF = 0.63, 40
 
 
 def run_reference(args, rank, world):

@@ -8,6 +8,8 @@ holds that system only.
 import numpy as np
 import pytest
 
+from conftest import rel_err
+
 pytestmark = pytest.mark.gpu
 
 
@@ -47,6 +49,30 @@ def test_each_system_equals_the_system_alone(pkg, ic, sizes):
             np.testing.assert_array_equal(a_ens[c][off[k]:off[k + 1]], a_one[c])
     assert st["p2p_pairs"] == pairs
     ens.close()
+
+
+def test_each_system_matches_the_oracle_on_that_system(pkg, ic, oracle):
+    """Pinned per system against the oracle, not only against the
+    single-system GPU path: every system of an uneven ensemble has the
+    oracle's accelerations (the reference's grouped walk at the same theta
+    and leaf capacity, FP64) and its interaction counts."""
+    sizes = (1024, 3000, 777, 2048)
+    parts = systems(ic, sizes, seed0=60)
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    with new_sim(pkg) as ens:
+        ens.set_particles(*concat(parts))
+        ens.set_ensemble(off)
+        ax, ay, az = ens.compute_accel()
+        st = ens.stats()
+    pairs = terms = 0
+    for k, (x, y, z, _, _, _, m) in enumerate(parts):
+        rx, ry, rz, cnt = oracle.bh_accel(x, y, z, m, 1.0, 0.01, 0.6, 16, counters=True)
+        sl = slice(off[k], off[k + 1])
+        e = rel_err(ax[sl], ay[sl], az[sl], rx, ry, rz)
+        assert np.median(e) <= 1e-5 and e.max() <= 1e-4, (k, np.median(e), e.max())
+        pairs += cnt["p2p_pairs"]
+        terms += cnt["p2c_terms"]
+    assert st["p2p_pairs"] == pairs and st["p2c_terms"] == terms
 
 
 def test_ensemble_kdk_and_checks(pkg, ic):
