@@ -533,6 +533,14 @@ def fp32_peak_detail(dev, probe, clk):
             "probe_frac_of_theoretical_max": probe / th(mx) if probe and mx else None}
 
 
+# DRAM bytes per particle of one radix-sort scatter pass at N = 4,194,304:
+# dram__bytes_read.sum + dram__bytes_write.sum of the six rs_scatter_kernel
+# launches of one sort (336.7 MB), a cold-cache ncu capture
+# (profiles/sort_scatter_galaxy4m.txt).  The keys and slots are L2-resident
+# between passes, so the traffic is below the algorithmic bytes.
+SORT_SCATTER_DRAM_BYTES_PER_PARTICLE_PASS = 13.4
+
+
 def sort_roofline(st, n, split):
     """The HBM-bound part of the tree build: the LSD radix sort (the
     evaluation's passes of 9-bit digits, up to 7; each reads and writes 8 B
@@ -545,7 +553,9 @@ def sort_roofline(st, n, split):
     peak, src = hbm_peak()
     ach = per * n / (ms * 1e-3) / 1e9 if ms > 0 else None
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
-            "traffic": None, "bytes_per_particle": per, "sort_passes": passes,
+            "traffic": SORT_SCATTER_DRAM_BYTES_PER_PARTICLE_PASS * passes * n,
+            "traffic_unit": "DRAM bytes of the phase's scatter passes (ncu bytes per particle-pass x passes x N)",
+            "bytes_per_particle": per, "sort_passes": passes,
             "kernel": "radix sort (rs_hist, rs_scatter) + permute",
             "peak_source": src}
 
