@@ -24,7 +24,7 @@ value   = N * K / (device time of the learned arm's K timed steps, CUDA
           arm's figure and the ratio are in config.
 e2e     = the same metric through the C-ABI with host buffers: per step
           ngrav_gpu_set_state_f32 from pinned host memory, ngrav_gpu_step(1),
-          ngrav_gpu_get_state into pinned FP64 arrays, wall clock (10 steps;
+          ngrav_gpu_get_state into pinned FP64 arrays, wall clock (20 steps;
           the three calls' shares are on the line).
 drift   = energy, momentum and angular-momentum drift of each arm over its
           timed steps (FP64 diagnostics; the potential is the exact pair sum
@@ -612,7 +612,7 @@ def main():
     ap.add_argument("--precision", default="split", choices=["split", "plain"])
     ap.add_argument("--leaf-grid", default="16,24,32,40,48,64",
                     help="leaf capacities tried per arm (comma list; one value fixes it)")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the compact records of the other BASELINE configs (C2, C3, C5)")
@@ -804,6 +804,7 @@ def main():
     parts = [1e3 * float(np.mean([p[i] for p in t_parts])) for i in range(3)]
     e2e = {"value": job_value(n, world, e2e_ms), "unit": "particle-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
            "d2h_bytes_per_step": 6 * 8 * n, "ms_per_step": e2e_ms, "steps": args.e2e_steps,
+           "ms_per_step_median": 1e3 * float(np.median(t_e2e)), "ms_per_step_max": 1e3 * float(np.max(t_e2e)),
            "ms_set_state": parts[0], "ms_step": parts[1], "ms_get_state": parts[2],
            "h2d_gbs": 6 * 4 * n / (parts[0] * 1e-3) / 1e9, "d2h_gbs": 6 * 8 * n / (parts[2] * 1e-3) / 1e9,
            "call": "ngrav_gpu_set_state_f32 + ngrav_gpu_step(1) + ngrav_gpu_get_state (pinned host buffers)"}
