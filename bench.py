@@ -535,10 +535,10 @@ def fp32_peak_detail(dev, probe, clk):
 
 # DRAM bytes per particle of one radix-sort scatter pass at N = 4,194,304:
 # dram__bytes_read.sum + dram__bytes_write.sum of the six rs_scatter_kernel
-# launches of one sort (336.7 MB), a cold-cache ncu capture
+# launches of one sort (329.9 MB), a cold-cache ncu capture
 # (profiles/sort_scatter_galaxy4m.txt).  The keys and slots are L2-resident
 # between passes, so the traffic is below the algorithmic bytes.
-SORT_SCATTER_DRAM_BYTES_PER_PARTICLE_PASS = 13.4
+SORT_SCATTER_DRAM_BYTES_PER_PARTICLE_PASS = 13.1
 
 
 def sort_roofline(st, n, split):
@@ -556,7 +556,7 @@ def sort_roofline(st, n, split):
             "traffic": SORT_SCATTER_DRAM_BYTES_PER_PARTICLE_PASS * passes * n,
             "traffic_unit": "DRAM bytes of the phase's scatter passes (ncu bytes per particle-pass x passes x N)",
             "bytes_per_particle": per, "sort_passes": passes,
-            "kernel": "radix sort (rs_hist, rs_scatter) + permute",
+            "kernel": "radix sort (rs_hist, rs_scan, rs_scatter) + permute",
             "peak_source": src}
 
 

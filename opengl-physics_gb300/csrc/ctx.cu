@@ -89,8 +89,7 @@ int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
     SortBuffers& S = ctx->SB;
     NG_CUDA(dalloc(S.keys, c)); NG_CUDA(dalloc(S.keys_alt, c)); NG_CUDA(dalloc(S.vals, c));
     NG_CUDA(dalloc(S.vals_alt, c));
-    const long long nb = (c + 4095) / 4096;
-    S.hist_cap = nb * kRsBins;
+    S.hist_cap = radix_hist_size(c);
     NG_CUDA(dalloc(S.hist, S.hist_cap));
     S.scan_tmp_cap = scan_tmp_size(std::max(S.hist_cap, c)) + 16;
     NG_CUDA(dalloc(S.scan_tmp, S.scan_tmp_cap));
@@ -224,10 +223,10 @@ void enqueue_eval(ngrav_gpu_ctx* ctx, bool bbox_ready, bool kick, float hdt) {
     radix_sort_pairs(ctx->SB, n, passes, 3 * kKeyLevels - kRsDigitBits * passes, s);
     ctx->sort_passes = passes;
     launch_permute(P, ctx->SB.vals, n, split, s);
-    // root, keys, 5 per sort pass (histogram, 3 scan kernels, scatter), permute,
+    // root, keys, 3 per sort pass (histogram, digit scans, scatter), permute,
     // tree init, the levels, leaf list (mark, 3 scan kernels, compact), leaf
     // moments, the internal-moment levels, walk
-    ctx->launches += 2 + (n > 1 ? 5 * passes : 0) + 1 + 1 + levels + 5 + 1 + levels + 1;
+    ctx->launches += 2 + (n > 1 ? 3 * passes : 0) + 1 + 1 + levels + 5 + 1 + levels + 1;
     std::swap(P.pos, P.pos2);
     std::swap(P.plo, P.plo2);
     std::swap(P.vel, P.vel2);

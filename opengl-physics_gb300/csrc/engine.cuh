@@ -262,6 +262,9 @@ int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, 
 // Stable LSD radix sort of (keys, vals) over bits [shift0, shift0 + kRsDigitBits*passes);
 // result ends in (keys, vals) (the alternates are scratch).
 void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cudaStream_t s);
+// Entries of SortBuffers::hist for n keys: the tile histograms, then the
+// digit totals.
+long long radix_hist_size(long long n);
 void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);
 void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s);
 // Builds levels 1 .. levels (keys sorted on their top `levels` digits); a node

@@ -470,54 +470,116 @@ void device_exclusive_scan(const unsigned* in, unsigned* out, long long n, unsig
 
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort, 9-bit digits (seven passes cover the 63-bit keys),
-// 4096-key tiles
+// tiles of 4096 keys (512 threads x 8); three kernels per pass (tile
+// histograms, per-digit scans over the tiles, scatter)
 // ---------------------------------------------------------------------------
 
-constexpr int kRsThreads = 256;
+constexpr int kRsThreads = 512;
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsItems = 16;
+constexpr int kRsItems = 8;
 constexpr int kRsTile = kRsThreads * kRsItems;   // 4096
-constexpr int kRsWarpSpan = 32 * kRsItems;       // 512 consecutive keys per warp
+constexpr int kRsWarpSpan = 32 * kRsItems;       // consecutive keys per warp
+constexpr int kRsScatterMinBlocks = 2;
 constexpr unsigned kRsMask = kRsBins - 1;
-static_assert(kRsBins == 2 * kRsThreads, "two digits per thread in the digit scans");
+constexpr int kRsDpt = kRsBins / kRsThreads;     // digits per thread in the digit scans
+static_assert(kRsDpt * kRsThreads == kRsBins, "whole digits per thread in the digit scans");
 
-// Histogram of one digit per tile, digit-major: hist[d * nblocks + b].
+// Lanes of the warp holding the same digit as this lane (the invalid lanes of
+// a ragged last tile form a group of their own): the AND of one ballot per
+// digit bit, cheaper than a warp match.
+__device__ __forceinline__ unsigned digit_peers(unsigned d, bool valid) {
+    const unsigned vb = __ballot_sync(0xffffffffu, valid);
+    unsigned peers = valid ? vb : ~vb;
+#pragma unroll
+    for (int b = 0; b < kRsDigitBits; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned bb = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? bb : ~bb;
+    }
+    return peers;
+}
+
+// Histogram of one digit per tile, digit-major: hist[d * nblocks + b].  All
+// keys of a thread are loaded before the first is counted; plain shared
+// atomics (a warp match to combine equal digits costs more than the
+// conflicts it saves).
 __global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const unsigned long long* __restrict__ keys,
                                                              long long n, int shift, unsigned* __restrict__ hist) {
     __shared__ unsigned h[kRsBins];
-    h[threadIdx.x] = 0;
-    h[threadIdx.x + kRsThreads] = 0;
-    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRsDpt; ++j) h[threadIdx.x + j * kRsThreads] = 0;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long long base = blockIdx.x * (long long)kRsTile + w * kRsWarpSpan + lane;
-#pragma unroll 4
+    unsigned d[kRsItems];
+#pragma unroll
     for (int k = 0; k < kRsItems; ++k) {
         const long long i = base + k * 32;
-        const unsigned d = i < n ? (unsigned)(keys[i] >> shift) & kRsMask : (unsigned)kRsBins;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (d < (unsigned)kRsBins && (__ffs(peers) - 1) == lane) atomicAdd(&h[d], (unsigned)__popc(peers));
+        d[k] = i < n ? (unsigned)(__ldg(keys + i) >> shift) & kRsMask : (unsigned)kRsBins;
     }
     __syncthreads();
-    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
-    hist[(threadIdx.x + kRsThreads) * gridDim.x + blockIdx.x] = h[threadIdx.x + kRsThreads];
+#pragma unroll
+    for (int k = 0; k < kRsItems; ++k) {
+        if (d[k] < (unsigned)kRsBins) atomicAdd(&h[d[k]], 1u);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRsDpt; ++j)
+        hist[(threadIdx.x + j * kRsThreads) * gridDim.x + blockIdx.x] = h[threadIdx.x + j * kRsThreads];
 }
 
-__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned long long* __restrict__ kin,
+// One block per digit d: exclusive scan over the tiles of row d of the
+// histogram, in place, and the row's total into totals[d].  The scatter adds
+// the digit's own offset (the exclusive scan of the totals) itself.
+__global__ void __launch_bounds__(kRsThreads) rs_scan_kernel(unsigned* __restrict__ hist, int nb,
+                                                             unsigned* __restrict__ totals) {
+    __shared__ unsigned s_warp[32];
+    unsigned* row = hist + (long long)blockIdx.x * nb;
+    constexpr int kPer = 4;
+    unsigned carry = 0;
+    for (int c0 = 0; c0 < nb; c0 += kRsThreads * kPer) {
+        const int i0 = c0 + threadIdx.x * kPer;
+        unsigned v[kPer];
+        unsigned sum = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            v[k] = i0 + k < nb ? row[i0 + k] : 0u;
+            sum += v[k];
+        }
+        unsigned total;
+        unsigned run = carry + block_exclusive_scan(sum, s_warp, total);
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            if (i0 + k < nb) row[i0 + k] = run;
+            run += v[k];
+        }
+        carry += total;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+// The tile's keys are ranked by digit in shared memory and written out in
+// digit runs.  The per-warp digit counters share the tile buffer (they are
+// dead once every key holds its rank), so a CTA holds 53 KB; at 64 registers
+// two CTAs of 512 threads share an SM.
+constexpr size_t kRsScatterSmem = (size_t)kRsTile * (sizeof(unsigned long long) + sizeof(unsigned));
+static_assert(kRsWarps * kRsBins * sizeof(unsigned) <= kRsScatterSmem, "digit counters fit the tile buffer");
+
+__global__ void __launch_bounds__(kRsThreads, kRsScatterMinBlocks) rs_scatter_kernel(const unsigned long long* __restrict__ kin,
                                                                 const unsigned* __restrict__ vin,
                                                                 unsigned long long* __restrict__ kout,
                                                                 unsigned* __restrict__ vout, long long n, int shift,
-                                                                const unsigned* __restrict__ hist_scan) {
+                                                                const unsigned* __restrict__ hist_scan,
+                                                                const unsigned* __restrict__ totals) {
     extern __shared__ unsigned long long rs_smem[];
-    unsigned long long* skeys = rs_smem;                          // kRsTile
+    unsigned long long* skeys = rs_smem;                             // kRsTile
     unsigned* svals = reinterpret_cast<unsigned*>(skeys + kRsTile);  // kRsTile
-    __shared__ unsigned warp_cnt[kRsWarps][kRsBins];
+    unsigned (*warp_cnt)[kRsBins] = reinterpret_cast<unsigned (*)[kRsBins]>(rs_smem);  // aliases skeys
     __shared__ unsigned digit_start[kRsBins];   // block-local exclusive prefix over digits
     __shared__ unsigned digit_base[kRsBins];    // global output offset of (digit, block)
     __shared__ unsigned s_warp[32];
 
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int k = threadIdx.x; k < kRsWarps * kRsBins; k += kRsThreads) (&warp_cnt[0][0])[k] = 0;
-    __syncthreads();
 
     const long long tile = blockIdx.x * (long long)kRsTile;
     const long long base = tile + w * kRsWarpSpan + lane;
@@ -531,8 +593,13 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
         const bool valid = i < n;
         key[k] = valid ? kin[i] : 0ull;
         val[k] = valid ? vin[i] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kRsItems; ++k) {
+        const bool valid = base + k * 32 < n;
         const unsigned d = valid ? (unsigned)(key[k] >> shift) & kRsMask : (unsigned)kRsBins;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned peers = digit_peers(d, valid);
         unsigned before = 0;
         if (valid) before = warp_cnt[w][d];
         __syncwarp();
@@ -543,33 +610,51 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
         __syncwarp();
     }
     __syncthreads();
-    // Per digit (thread t: digits 2t, 2t+1): exclusive prefix over warps
-    // (stable: warp w precedes w+1), then over digits.
-    const unsigned d0 = 2 * threadIdx.x, d1 = d0 + 1;
-    unsigned run0 = 0, run1 = 0;
+    // Per digit (thread t: digits kRsDpt t ...): exclusive prefix over warps
+    // (stable: warp w precedes w+1), then over digits; the digit's global
+    // offset is the scan of the digit totals plus this tile's row prefix.
+    unsigned run[kRsDpt], tot[kRsDpt];
+    unsigned rsum = 0, tsum = 0;
 #pragma unroll
-    for (int ww = 0; ww < kRsWarps; ++ww) {
-        const unsigned c0 = warp_cnt[ww][d0], c1 = warp_cnt[ww][d1];
-        warp_cnt[ww][d0] = run0;
-        warp_cnt[ww][d1] = run1;
-        run0 += c0;
-        run1 += c1;
+    for (int j = 0; j < kRsDpt; ++j) {
+        const unsigned d = kRsDpt * threadIdx.x + j;
+        run[j] = 0;
+#pragma unroll
+        for (int ww = 0; ww < kRsWarps; ++ww) {
+            const unsigned c = warp_cnt[ww][d];
+            warp_cnt[ww][d] = run[j];
+            run[j] += c;
+        }
+        tot[j] = __ldg(totals + d);
+        rsum += run[j];
+        tsum += tot[j];
     }
     unsigned total;
-    const unsigned ds = block_exclusive_scan(run0 + run1, s_warp, total);
-    digit_start[d0] = ds;
-    digit_start[d1] = ds + run0;
-    digit_base[d0] = hist_scan[d0 * gridDim.x + blockIdx.x];
-    digit_base[d1] = hist_scan[d1 * gridDim.x + blockIdx.x];
+    unsigned ds = block_exclusive_scan(rsum, s_warp, total);
+    unsigned gs = block_exclusive_scan(tsum, s_warp, total);
+#pragma unroll
+    for (int j = 0; j < kRsDpt; ++j) {
+        const unsigned d = kRsDpt * threadIdx.x + j;
+        digit_start[d] = ds;
+        digit_base[d] = gs + hist_scan[d * gridDim.x + blockIdx.x];
+        ds += run[j];
+        gs += tot[j];
+    }
+    __syncthreads();
+    // every key's place in the tile, then (counters dead) the tile itself
+#pragma unroll
+    for (int k = 0; k < kRsItems; ++k) {
+        if (base + k * 32 < n) {
+            const unsigned dd = (unsigned)(key[k] >> shift) & kRsMask;
+            rank[k] = (unsigned short)(digit_start[dd] + warp_cnt[w][dd] + rank[k]);
+        }
+    }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kRsItems; ++k) {
-        const long long i = base + k * 32;
-        if (i < n) {
-            const unsigned dd = (unsigned)(key[k] >> shift) & kRsMask;
-            const unsigned r = digit_start[dd] + warp_cnt[w][dd] + rank[k];
-            skeys[r] = key[k];
-            svals[r] = val[k];
+        if (base + k * 32 < n) {
+            skeys[rank[k]] = key[k];
+            svals[rank[k]] = val[k];
         }
     }
     __syncthreads();
@@ -584,15 +669,17 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(const unsigned l
     }
 }
 
+long long radix_hist_size(long long n) { return ((n + kRsTile - 1) / kRsTile + 1) * kRsBins; }
+
 void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cudaStream_t s) {
     if (n <= 1) return;
     const int nb = (int)((n + kRsTile - 1) / kRsTile);
-    const size_t smem = (size_t)kRsTile * (sizeof(unsigned long long) + sizeof(unsigned));
     static bool attr_done = false;
     if (!attr_done) {
-        cudaFuncSetAttribute(rs_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(rs_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRsScatterSmem);
         attr_done = true;
     }
+    unsigned* totals = sb.hist + (long long)nb * kRsBins;
     unsigned long long* kin = sb.keys;
     unsigned long long* kout = sb.keys_alt;
     unsigned* vin = sb.vals;
@@ -600,8 +687,8 @@ void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cuda
     for (int p = 0; p < passes; ++p) {
         const int shift = shift0 + kRsDigitBits * p;
         rs_hist_kernel<<<nb, kRsThreads, 0, s>>>(kin, n, shift, sb.hist);
-        device_exclusive_scan(sb.hist, sb.hist, (long long)nb * kRsBins, sb.scan_tmp, s);
-        rs_scatter_kernel<<<nb, kRsThreads, smem, s>>>(kin, vin, kout, vout, n, shift, sb.hist);
+        rs_scan_kernel<<<kRsBins, kRsThreads, 0, s>>>(sb.hist, nb, totals);
+        rs_scatter_kernel<<<nb, kRsThreads, kRsScatterSmem, s>>>(kin, vin, kout, vout, n, shift, sb.hist, totals);
         unsigned long long* tk = kin;
         kin = kout;
         kout = tk;
