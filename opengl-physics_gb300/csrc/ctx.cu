@@ -93,7 +93,7 @@ int alloc_particles(ngrav_gpu_ctx* ctx, long long n) {
     NG_CUDA(dalloc(S.hist, S.hist_cap));
     S.scan_tmp_cap = scan_tmp_size(std::max(S.hist_cap, c)) + 16;
     NG_CUDA(dalloc(S.scan_tmp, S.scan_tmp_cap));
-    NG_CUDA(dalloc(S.ktab, 3 * (long long)kKeyTabSize));
+    NG_CUDA(dalloc(S.ktab, key_table_entries()));
     S.cap = c;
     NG_CUDA(dalloc(ctx->leaf_at, c)); NG_CUDA(dalloc(ctx->flags, c)); NG_CUDA(dalloc(ctx->scanbuf, c));
     NG_CUDA(dalloc(ctx->leaf_list, c)); NG_CUDA(dalloc(ctx->inv, c));

@@ -22,8 +22,6 @@
 namespace ngrav {
 
 constexpr int kKeyLevels = 21;          // 63-bit keys: 3 bits per level
-constexpr int kKeyTabLevels = 14;       // key levels whose centres are tabulated per build
-constexpr int kKeyTabSize = 1 << kKeyTabLevels;  // table entries per axis (entry 0 unused)
 constexpr int kRsDigitBits = 9;         // radix sort digit: 7 passes over the 63-bit keys
 constexpr int kRsBins = 1 << kRsDigitBits;
 constexpr int kRsPasses = (3 * kKeyLevels + kRsDigitBits - 1) / kRsDigitBits;
@@ -163,7 +161,7 @@ struct SortBuffers {
     unsigned* scan_tmp = nullptr;
     long long hist_cap = 0;
     long long scan_tmp_cap = 0;
-    double* ktab = nullptr;           // centres of the top key levels, 3 x kKeyTabSize
+    double* ktab = nullptr;           // centres of the top key levels (key_table_entries())
 };
 
 struct WalkParams {
@@ -256,7 +254,7 @@ void launch_forest_bbox(const float4* pos, const float4* plo, long long n, const
 void launch_forest_root(const Forest& F, cudaStream_t s);
 void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s);
 // Keys of the current order (vals = 0 .. n-1); a single system also fills
-// the centre table ktab (3 * kKeyTabSize doubles).  Returns the launches made.
+// the centre table ktab (key_table_entries() doubles).  Returns the launches made.
 int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
 // Stable LSD radix sort of (keys, vals) over bits [shift0, shift0 + kRsDigitBits*passes);
@@ -265,6 +263,8 @@ void radix_sort_pairs(SortBuffers& sb, long long n, int passes, int shift0, cuda
 // Entries of SortBuffers::hist for n keys: the tile histograms, then the
 // digit totals.
 long long radix_hist_size(long long n);
+// Doubles of SortBuffers::ktab: the tabulated key centres of the three axes.
+long long key_table_entries();
 void launch_permute(const Particles& P, const unsigned* perm, long long n, bool split, cudaStream_t s);
 void launch_tree_init(NodeArrays& T, Counters* C, long long n, int leaf_cap, int max_depth, cudaStream_t s);
 // Builds levels 1 .. levels (keys sorted on their top `levels` digits); a node

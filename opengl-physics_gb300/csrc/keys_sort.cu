@@ -239,26 +239,57 @@ __device__ __forceinline__ unsigned axis_bits(double p, double c, double h) {
     return bits;
 }
 
+constexpr int kKeyTabLevels = 17;                // key levels whose centres are tabulated per build
+constexpr int kKeyTabSize = 1 << kKeyTabLevels;  // table entries per axis (entry 0 unused)
+constexpr int kKeySub = 4;                       // levels a table thread fills below its own entry
+constexpr int kKeyTop = kKeyTabLevels - 1 - kKeySub;  // level of those threads' entries
+static_assert(kKeyTop >= 0, "the table is deeper than one thread's subtree");
+
+long long key_table_entries() { return 3LL * kKeyTabSize; }
+
+__device__ __forceinline__ double centre_step(double c, long long hb, bool up) {
+    return __dadd_rn(c, __longlong_as_double(up ? hb : (hb | (long long)0x8000000000000000ull)));
+}
+
 // The centre recurrence of an axis depends only on that axis's own octant
 // bits, so the centres of levels 0 .. kKeyTabLevels-1 are tabulated once per
 // build: an implicit binary tree per axis, entry 1 the root centre and entry
-// 2e + b the child of entry e on side b (b = 1: p >= c).  Each entry replays
-// exactly the FP64 additions of the walk down to it, so the keys kernel looks
-// the top levels up and adds in FP64 only below them (7 additions per axis
-// instead of 21).
+// 2e + b the child of entry e on side b (b = 1: p >= c).  Every entry is the
+// exact FP64 sequence of additions of the walk down to it, so the keys kernel
+// looks the top levels up and adds in FP64 only below them.  One thread per
+// entry of level kKeyTop replays the walk to it and derives its subtree
+// kKeySub levels down, one addition per entry from the parent's value (the
+// same operands and rounding as the walk); one thread per entry above
+// kKeyTop replays its own walk.
 __global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restrict__ C, double* __restrict__ tab) {
+    constexpr int nroot = 1 << kKeyTop;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 3 * kKeyTabSize) return;
-    const int axis = i / kKeyTabSize, e = i % kKeyTabSize;
+    const bool sub = i < 3 * nroot;
+    const int j = sub ? i : i - 3 * nroot;
+    if (j >= 3 * nroot) return;
+    const int axis = j / nroot;
+    const int e = sub ? nroot + j % nroot : j % nroot;  // an entry of level kKeyTop, or one above it
     if (e == 0) return;
     const int l = 31 - __clz(e);  // level of entry e: its bits below the leading one are levels 0 .. l-1
     double c = C->root_center[axis];
     long long hb = __double_as_longlong(C->root_half);
     for (int k = l - 1; k >= 0; --k) {
         hb -= 1ll << 52;
-        c = __dadd_rn(c, __longlong_as_double((e >> k) & 1 ? hb : (hb | (long long)0x8000000000000000ull)));
+        c = centre_step(c, hb, (e >> k) & 1);
     }
-    tab[i] = c;
+    double* t = tab + (long long)axis * kKeyTabSize;
+    t[e] = c;
+    if (!sub) return;
+    double lv[1 << kKeySub];  // the subtree's centres of one level, left to right
+    lv[0] = c;
+#pragma unroll
+    for (int d = 1; d <= kKeySub; ++d) {
+        hb -= 1ll << 52;
+#pragma unroll
+        for (int q = (1 << d) - 1; q >= 0; --q) lv[q] = centre_step(lv[q >> 1], hb, q & 1);
+#pragma unroll
+        for (int q = 0; q < (1 << d); ++q) t[(e << d) + q] = lv[q];
+    }
 }
 
 // axis_bits over all kKeyLevels levels with the top kKeyTabLevels looked up
@@ -356,7 +387,7 @@ int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, 
     const unsigned g = (unsigned)blocks;
     switch (F.sys_levels) {
         case 0:
-            key_table_kernel<<<(3 * kKeyTabSize + 255) / 256, 256, 0, s>>>(C, ktab);
+            key_table_kernel<<<(6 * (1 << kKeyTop) + 255) / 256, 256, 0, s>>>(C, ktab);
             keys_kernel<<<g, 256, 0, s>>>(pos, plo, n, C, ktab, keys, vals);
             return 2;
         case 1: forest_keys_kernel<1><<<g, 256, 0, s>>>(pos, plo, n, F, keys, vals); break;
