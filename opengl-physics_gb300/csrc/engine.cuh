@@ -161,7 +161,7 @@ struct SortBuffers {
     unsigned* scan_tmp = nullptr;
     long long hist_cap = 0;
     long long scan_tmp_cap = 0;
-    double* ktab = nullptr;           // centres of the top key levels (key_table_entries())
+    long long* ktab = nullptr;        // centres of the top key levels, ordered images (key_table_entries())
 };
 
 struct WalkParams {
@@ -255,7 +255,7 @@ void launch_forest_root(const Forest& F, cudaStream_t s);
 void launch_collapse_split(float4* pos, float4* plo, long long n, cudaStream_t s);
 // Keys of the current order (vals = 0 .. n-1); a single system also fills
 // the centre table ktab (key_table_entries() doubles).  Returns the launches made.
-int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
+int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, long long* ktab,
                 unsigned long long* keys, unsigned* vals, cudaStream_t s);
 // Stable LSD radix sort of (keys, vals) over bits [shift0, shift0 + kRsDigitBits*passes);
 // result ends in (keys, vals) (the alternates are scratch).

@@ -260,8 +260,9 @@ __device__ __forceinline__ double centre_step(double c, long long hb, bool up) {
 // entry of level kKeyTop replays the walk to it and derives its subtree
 // kKeySub levels down, one addition per entry from the parent's value (the
 // same operands and rounding as the walk); one thread per entry above
-// kKeyTop replays its own walk.
-__global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restrict__ C, double* __restrict__ tab) {
+// kKeyTop replays its own walk.  Entries are stored as their ordered bit
+// images (ordered_bits), the form the keys kernel compares.
+__global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restrict__ C, long long* __restrict__ tab) {
     constexpr int nroot = 1 << kKeyTop;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool sub = i < 3 * nroot;
@@ -277,8 +278,8 @@ __global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restri
         hb -= 1ll << 52;
         c = centre_step(c, hb, (e >> k) & 1);
     }
-    double* t = tab + (long long)axis * kKeyTabSize;
-    t[e] = c;
+    long long* t = tab + (long long)axis * kKeyTabSize;
+    t[e] = ordered_bits(c);
     if (!sub) return;
     double lv[1 << kKeySub];  // the subtree's centres of one level, left to right
     lv[0] = c;
@@ -288,21 +289,27 @@ __global__ void __launch_bounds__(256) key_table_kernel(const Counters* __restri
 #pragma unroll
         for (int q = (1 << d) - 1; q >= 0; --q) lv[q] = centre_step(lv[q >> 1], hb, q & 1);
 #pragma unroll
-        for (int q = 0; q < (1 << d); ++q) t[(e << d) + q] = lv[q];
+        for (int q = 0; q < (1 << d); ++q) t[(e << d) + q] = ordered_bits(lv[q]);
     }
 }
 
+// The double of an ordered bit image (a -0 centre comes back as +0, which
+// gives the same sums with the nonzero halves added to it).
+__device__ __forceinline__ double from_ordered(long long o) {
+    return __longlong_as_double(o ^ ((o >> 63) & 0x7FFFFFFFFFFFFFFFll));
+}
+
 // axis_bits over all kKeyLevels levels with the top kKeyTabLevels looked up
-// in the axis's table.
-__device__ __forceinline__ unsigned axis_bits_tab(double p, const double* __restrict__ tab, double h0) {
+// in the axis's table of ordered images.
+__device__ __forceinline__ unsigned axis_bits_tab(double p, const long long* __restrict__ tab, double h0) {
     const long long op = ordered_bits(p);
     unsigned e = 1;
 #pragma unroll
-    for (int l = 0; l < kKeyTabLevels; ++l) e = 2 * e + (op >= ordered_bits(__ldg(tab + e)) ? 1u : 0u);
+    for (int l = 0; l < kKeyTabLevels; ++l) e = 2 * e + (op >= __ldg(tab + e) ? 1u : 0u);
     // continue from the centre of level kKeyTabLevels: the last tabulated
     // centre plus or minus h / 2^kKeyTabLevels, as the recurrence would
     long long hb = __double_as_longlong(h0) - ((long long)kKeyTabLevels << 52);
-    double c = __dadd_rn(__ldg(tab + (e >> 1)),
+    double c = __dadd_rn(from_ordered(__ldg(tab + (e >> 1))),
                          __longlong_as_double(e & 1 ? hb : (hb | (long long)0x8000000000000000ull)));
     unsigned bits = e - (1u << kKeyTabLevels);
 #pragma unroll
@@ -330,7 +337,7 @@ __device__ __forceinline__ unsigned long long spread3(unsigned v) {
 
 __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ pos, const float4* __restrict__ plo,
                                                    long long n, const Counters* __restrict__ C,
-                                                   const double* __restrict__ tab,
+                                                   const long long* __restrict__ tab,
                                                    unsigned long long* __restrict__ keys,
                                                    unsigned* __restrict__ vals) {
     const double h0 = C->root_half;
@@ -379,7 +386,7 @@ __global__ void __launch_bounds__(256) forest_keys_kernel(const float4* __restri
     }
 }
 
-int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, double* ktab,
+int launch_keys(const float4* pos, const float4* plo, long long n, Counters* C, const Forest& F, long long* ktab,
                 unsigned long long* keys, unsigned* vals, cudaStream_t s) {
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
