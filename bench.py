@@ -419,7 +419,7 @@ BUDGET_GRID = (5e-5, 1e-4, 1.5e-4, 2e-4, 2.5e-4, 2.75e-4, 3e-4, 3.1e-4, 3.2e-4, 
                3.7e-4, 3.8e-4, 3.9e-4, 4e-4, 4.5e-4, 5e-4, 7e-4, 1e-3)
 TARGET_RMS = 1e-3
 # The learned test's in-run safety check: every 10 steps an FP64-summed
-# direct sum on this many sampled targets judges the rms error (about +-3 %
+# direct sum on this many sampled targets estimates the rms error (about +-3 %
 # on the rms at 1,024 targets), reverting to the theta test above 1.5x the
 # target.  The error reported on the line is measured separately, on 4,096.
 CHECK_TARGETS = 1024
